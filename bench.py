@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""SPH particle-steps/s of the 3D block collapse (1,048,576 particles) on one GB300.
+
+One "step" is one oclFluid3D::compute() of the whole scene: hash, one-sweep sort (+reorder),
+cell bounds, density, forces + integration. Default: N=1 GPU, 1000 timed steps after 5
+warm-up steps, L2 flushed (512 MiB write) between timed steps, each step timed with CUDA
+events on the stream it runs on. Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU port of the reference's kernels (the oracle; the reference's
+OpenCL kernels cannot run here) on the host cores, on a bounded sample of the same scene.
+With N>1 (torchrun) the plain step does not shard: every rank advances its own replica.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SPH particle-steps/s, 1M 3D block collapse (plain step)"
+UNIT = "particle-steps/s"
+L2_FLUSH_BYTES = 512 << 20
+
+# Algorithmic bytes per particle per launch of each stage of the fused LINEAR_GRID step
+# (each array counted once per stage; neighbour re-reads and the per-brick cell-table reads
+# are not counted). Stated with their derivation in the design doc.
+STAGE_BYTES_PER_PARTICLE = {
+    "front_end": 16 + 4 + 4,          # R pos, W key, R previous sorted key (sparse table clear)
+    "sort": 12 + 16 + 80,             # pass0 R key W key,val; pass1 R/W key,val; pass2 + gather pos,vel
+    "bounds": 4,                      # R sorted key (+8 B per occupied cell, added below)
+    "density": 16 + 16 + 4,           # R spos, W spos (w = density), W svel.w
+    "forces": 16 + 16 + 4 + 32 + 32 + 32,  # R spos,svel,index; R/W pos, vel, force
+}
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "100"]
+        if self.gpu_id:
+            cmd += ["-i", self.gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            time.sleep(0.15)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self._t:
+                self._t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def gpu_ident(torch) -> str | None:
+    try:
+        props = torch.cuda.get_device_properties(torch.cuda.current_device())
+        u = getattr(props, "uuid", None)
+        if u is not None:
+            s = str(u)
+            return s if s.startswith("GPU-") else "GPU-" + s
+    except Exception:
+        pass
+    return None
+
+
+def load_scene(fluid, scene):
+    import ctypes
+    import torch
+    from libcl_gb300 import Fluid3DParams
+    fluid.compile()
+    fluid.setParticleCount(scene.n)
+    ctypes.memmove(ctypes.byref(fluid.getParameters()), ctypes.byref(scene.params), ctypes.sizeof(Fluid3DParams))
+    fluid.getPositionBuffer().copy_(torch.from_numpy(scene.pos))
+    fluid.getVelocityBuffer().copy_(torch.from_numpy(scene.vel))
+    fluid.getForceBuffer().zero_()
+    torch.cuda.synchronize()
+
+
+def cpu_baseline(scene, seconds: float = 10.0):
+    """The oracle (CPU port of the reference kernels, restated 4-bit reference sort) on the
+    full scene, all host threads, for about `seconds` of work."""
+    import oracle
+    pos, vel, force = scene.pos.copy(), scene.vel.copy(), np.zeros_like(scene.pos)
+    oracle.step(pos, vel, force, scene.params, ref_sort=True)  # warm-up (page-in, thread pool)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.step(pos, vel, force, scene.params, ref_sort=True)
+        steps += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds or steps >= 50:
+            break
+    return {"value": scene.n * steps / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+            "sample": f"{steps} full steps of the {scene.n}-particle scene ({dt:.1f} s)"}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU port of the reference kernels on a bounded sample."""
+    if rank != 0:
+        return 0
+    import oracle
+    from libcl_gb300.scenes import block_collapse_3d
+    sample = block_collapse_3d(32, 32, 32)  # 32,768 particles of the same lattice, same parameters
+    pos, vel, force = sample.pos.copy(), sample.vel.copy(), np.zeros_like(sample.pos)
+    for _ in range(args.warmup):
+        oracle.step(pos, vel, force, sample.params, ref_sort=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.step(pos, vel, force, sample.params, ref_sort=True)
+    dt = time.perf_counter() - t0
+    value = sample.n * args.steps / dt
+    cores = oracle.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded jittered lattice)",
+        "config": {"workload": "3d_block_collapse_1M", "sample_particles": sample.n,
+                   "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample.n}-particle 32x32x32 sub-block of the scene, {args.steps} steps"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--quick", action="store_true", help="skip e2e/profile/baseline legs (for ncu)")
+    args = ap.parse_args(argv)
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if args.warmup < 3:
+        print("warmup must be >= 3", file=sys.stderr)
+        return 2
+
+    import torch
+    import torch.distributed as dist
+    from libcl_gb300 import OPT_PROFILE, Fluid3D
+    from libcl_gb300.scenes import block_collapse_3d
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    scene = block_collapse_3d()
+    fluid = Fluid3D()
+    load_scene(fluid, scene)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    for _ in range(args.warmup):
+        fluid.compute(stream)
+    torch.cuda.synchronize()
+    assert fluid.sync_status() == 0, fluid.last_error()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(gpu_ident(torch)) as clocks:
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            fluid.compute(stream)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    t_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    status = fluid.sync_status()
+    if status != 0:
+        print(f"device status {status}: {fluid.last_error()}", file=sys.stderr)
+        return 1
+    value = scene.n * args.steps * world / (t_ms * 1e-3)
+    launches_per_step = 7  # hash, 3 sort passes, bounds, density, forces
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded jittered lattice, block_collapse_3d seed 2)",
+        "config": {"workload": "3d_block_collapse_1M", "particles": scene.n, "lattice": [128, 64, 128],
+                   "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5, "parallelism": f"replicas x{world}",
+                   "l2": "flushed between timed steps (512 MiB write)", "graph": True},
+        "gpu_launches": launches_per_step * args.steps,
+        "step_ms_p50": statistics.median(step_ms),
+    }
+    cs = clocks.summary()
+    result["clocks"] = cs
+
+    if not args.quick and rank == 0:
+        # per-stage events on the launching stream (eager replay of the same fused kernels)
+        fluid.set_option(OPT_PROFILE, 1)
+        acc: dict[str, list[float]] = {}
+        n_cells_occ = None
+        for _ in range(20):
+            flush.zero_()
+            fluid.compute(stream)
+            for k, v in fluid.stage_times().items():
+                acc.setdefault(k, []).append(v)
+        fluid.set_option(OPT_PROFILE, 0)
+        cell = fluid.getCellBuffer()
+        n_cells_occ = int((cell[1:] != cell[:-1]).sum().item()) + 1
+        stage_ms = {k: statistics.median(v) for k, v in acc.items()}
+        peak, peak_kind = measured_peaks()
+        stage_gbs = {}
+        for k, ms in stage_ms.items():
+            b = STAGE_BYTES_PER_PARTICLE[k] * scene.n + (8 * n_cells_occ if k == "bounds" else 0)
+            stage_gbs[k] = b / (ms * 1e-3) / 1e9
+        dom = max(stage_ms, key=stage_ms.get)
+        dom_bytes = STAGE_BYTES_PER_PARTICLE[dom] * scene.n
+        ach = stage_gbs[dom]
+        traffic = None
+        tp = ROOT / "profiles" / "traffic.json"
+        if tp.exists():
+            traffic = json.loads(tp.read_text()).get(dom)
+        result["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                              "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
+                              "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": stage_ms[dom]}
+        step_bytes = sum(STAGE_BYTES_PER_PARTICLE.values()) * scene.n + 8 * n_cells_occ
+        result["stages"] = {"ms": stage_ms, "gbs": stage_gbs, "occupied_cells": n_cells_occ,
+                            "step_algorithmic_bytes": step_bytes,
+                            "step_hbm_frac": step_bytes / (t_ms / args.steps * 1e-3) / 1e9 / peak}
+
+        # end to end through the C ABI with host buffers: H2D of the step's inputs
+        # (position, velocity, force) from pinned memory, compute, D2H of the result.
+        from libcl_gb300 import BUF_FORCE, BUF_POSITION, BUF_VELOCITY
+        hp = [torch.empty((scene.n, 4), dtype=torch.float32, pin_memory=True) for _ in range(3)]
+        for h, w in zip(hp, (BUF_POSITION, BUF_VELOCITY, BUF_FORCE)):
+            h.copy_(fluid.buffer(w).cpu())
+        dev = [fluid.buffer(w) for w in (BUF_POSITION, BUF_VELOCITY, BUF_FORCE)]
+        k_e2e = min(args.steps, 200)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(k_e2e):
+            for h, d in zip(hp, dev):
+                d.copy_(h, non_blocking=True)
+            fluid.compute(stream)
+            for h, d in zip(hp, dev):
+                h.copy_(d, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1)
+        result["e2e"] = {"value": scene.n * k_e2e / (e2e_ms * 1e-3), "unit": UNIT,
+                         "h2d_bytes_per_step": 3 * 16 * scene.n, "d2h_bytes_per_step": 3 * 16 * scene.n,
+                         "steps": k_e2e}
+        if world == 1 and not args.no_cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

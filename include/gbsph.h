@@ -1,0 +1,236 @@
+/*
+ * gbsph.h -- C ABI of the GB300 (sm_103a) SPH fluid step and the stable radix sort it uses.
+ *
+ * Every entry point takes plain pointers, sizes and an opaque CUDA stream (`void*`, a
+ * cudaStream_t; NULL = the legacy default stream). Device pointers are CUDA device
+ * addresses on the handle's device. Status codes are ints: 0 = success, negative = error.
+ * No C++ exceptions cross this boundary. Handles are independent (no global mutable state
+ * apart from the optional log sink), and each handle must be used from one host thread at
+ * a time.
+ *
+ * The reference interface each entry point replaces is cited as `libCL/<file>:<line>`
+ * (jochenstier/libcl, an OpenCL 1.x library).
+ */
+#ifndef GBSPH_H
+#define GBSPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBSPH_API __attribute__((visibility("default")))
+#else
+#define GBSPH_API
+#endif
+
+/* ------------------------------------------------------------------------------------------
+ * Status codes. Replace the reference's int/bool returns plus the global `sStatusCL`
+ * (libCL/oclCommon.cpp:19, libCL/oclCommon.h:36-38).
+ * ---------------------------------------------------------------------------------------- */
+enum {
+    GBSPH_OK = 0,
+    GBSPH_ERR_ARGUMENT = -1,        /* null handle/pointer, bad enum, NaN parameter */
+    GBSPH_ERR_SIZE_MISMATCH = -2,   /* key/value counts differ, borrowed buffer too small */
+    GBSPH_ERR_TOO_LARGE = -3,       /* element count beyond what the kernels address */
+    GBSPH_ERR_BIT_RANGE = -4,       /* (end_bit - start_bit) not a multiple of 4, or outside [0,32] */
+    GBSPH_ERR_CUDA = -5,            /* a CUDA runtime call failed; see *_last_error() */
+    GBSPH_ERR_DEVICE_TIMEOUT = -6,  /* a bounded device-side wait (look-back, mbarrier) gave up */
+    GBSPH_ERR_NOT_COMPILED = -7,    /* compute() before compile() */
+    GBSPH_ERR_OUT_OF_MEMORY = -8,
+    GBSPH_ERR_DEVICE_RANGE = -9,    /* a key/cell index fell outside its table on the device */
+    GBSPH_ERR_STATE = -10           /* call not valid in the current state */
+};
+
+/* Human-readable name of a status code (static storage). */
+GBSPH_API const char* gbsph_status_string(int status);
+
+/* ABI version: major*10000 + minor*100 + patch. */
+GBSPH_API int gbsph_version(void);
+
+/* Log sink. Replaces the reference's replaceable `ERR/WARN/INFO/KERNEL` function pointers
+ * (libCL/oclCommon.h:40-44, libCL/oclCommon.cpp:82-85). level: 0=ERR 1=WARN 2=INFO. */
+typedef void (*gbsph_log_fn)(int level, const char* message, void* user);
+GBSPH_API void gbsph_set_logger(gbsph_log_fn fn, void* user);
+
+/* ------------------------------------------------------------------------------------------
+ * Radix sort. Replaces `oclRadixSort` (libCL/sort/oclRadixSort.h:22-49):
+ *   oclRadixSort(oclContext&, oclProgram* parent)        -> gbsph_radix_sort_create
+ *   int compute(oclDevice&, oclBuffer& key, oclBuffer& val, int startBit, int endBit)
+ *                                                         -> gbsph_radix_sort_compute
+ *                                          (libCL/sort/oclRadixSort.cpp:62-144)
+ * Semantics kept: a stable LSD sort of (uint32 key, uint32 value) pairs on key bits
+ * [start_bit, end_bit), in place; key and value counts must match; (end_bit - start_bit)
+ * must be a multiple of 4. Deviation: the reference rejects n >= 4,194,304
+ * (libCL/sort/oclRadixSort.cpp:24,70-74); this sort accepts n < 2^30.
+ * The handle owns temporary buffers that grow to the largest n seen (the reference's
+ * `fit()`, libCL/sort/oclRadixSort.cpp:50-59).
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbsph_radix_sort_s* gbsph_radix_sort_t;
+
+GBSPH_API int gbsph_radix_sort_create(gbsph_radix_sort_t* out);
+GBSPH_API int gbsph_radix_sort_destroy(gbsph_radix_sort_t h);
+GBSPH_API int gbsph_radix_sort_compute(gbsph_radix_sort_t h, uint32_t* keys, uint32_t* values,
+                                       size_t n_keys, size_t n_values, int start_bit,
+                                       int end_bit, void* stream);
+/* Cell start/end extraction over sorted keys: fills both tables with 0xFFFFFFFF, then
+ * cell_start[k] = first index of key k, cell_end[k] = one past its last index.
+ * Replaces the fill + `clFindBounds` pair (libCL/phys/oclFluid3D.cpp:309-315,
+ * libCL/phys/oclFluid3D.cl:85-113). Keys >= n_cells are skipped on the device and reported
+ * as GBSPH_ERR_DEVICE_RANGE by gbsph_radix_sort_sync_status. */
+GBSPH_API int gbsph_radix_sort_cell_bounds(gbsph_radix_sort_t h, const uint32_t* sorted_keys,
+                                           size_t n, uint32_t* cell_start, uint32_t* cell_end,
+                                           size_t n_cells, void* stream);
+/* Synchronises `stream`, then reports (and clears) the handle's device-side error word. */
+GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream);
+GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h);
+
+/* ------------------------------------------------------------------------------------------
+ * 3D SPH fluid. Replaces `oclFluid3D` (libCL/phys/oclFluid3D.h:21-123,
+ * libCL/phys/oclFluid3D.cpp:21-342).
+ * ---------------------------------------------------------------------------------------- */
+
+/* Key modes. REFERENCE_HASH reproduces `hashKey` (libCL/phys/oclFluid3D.cl:44-52): the
+ * Teschner XOR hash of the integer cell, modulo 262144 buckets, including the double visits
+ * of colliding buckets in the 27-cell loops. LINEAR_GRID keys a bounded grid as
+ * x + nx*(y + ny*z) with cell coordinates clamped to the grid (no collisions). */
+enum { GBSPH_KEY_REFERENCE_HASH = 0, GBSPH_KEY_LINEAR_GRID = 1 };
+
+/* Mirrors `oclFluid3D::Params` (libCL/phys/oclFluid3D.h:48-63) field for field, followed by
+ * the values the reference hard-codes as kernel arguments (gravity, clip box:
+ * libCL/phys/oclFluid3D.cpp:256-268) and the key-grid description. */
+typedef struct gbsph_fluid3d_params {
+    float deltaTime;
+    float particleRadius;
+    float cellSize;
+    float mass;
+    float viscosity;
+    float pressure;
+    float density;
+    float spacing;
+    float stiffness;
+    float viscosityConstant;
+    float pressureConstant;
+    float kernelConstant;
+    float velocitylimit;
+    /* extensions (not in the reference struct) */
+    float gravity[4];    /* value the gravity stage writes into every force; the reference
+                            writes -9.8f * (0,0,1,0) */
+    float boxMin[4];     /* clip box, reference: (-1,-1,-1,0) */
+    float boxMax[4];     /* clip box, reference: ( 1, 1, 1,0) */
+    float gridOrigin[4]; /* LINEAR_GRID: cell = floor((pos - origin) / cellSize) */
+    int32_t gridDim[4];  /* LINEAR_GRID: nx, ny, nz (w unused) */
+    int32_t keyMode;     /* GBSPH_KEY_* */
+    int32_t dims;        /* 3 (default) or 2: 9 neighbour cells, z ignored, x/y walls only */
+    int32_t reserved[2];
+} gbsph_fluid3d_params;
+
+/* Buffers, by role. Position/velocity/force are float4[N] in particle order (settable,
+ * `setPositionBuffer` etc., libCL/phys/oclFluid3D.cpp:131-165). The sorted buffers are
+ * float4[N] in cell order: after compute(), sorted position .w = density and sorted
+ * velocity .w = pressure (libCL/phys/oclFluid3D.cl:192-198). INDEX maps sorted slot ->
+ * particle (uint32[N]); CELL holds the sorted keys (uint32[N]). */
+enum {
+    GBSPH_BUF_POSITION = 0,
+    GBSPH_BUF_VELOCITY = 1,
+    GBSPH_BUF_FORCE = 2,
+    GBSPH_BUF_SORTED_POSITION = 3,
+    GBSPH_BUF_SORTED_VELOCITY = 4,
+    GBSPH_BUF_INDEX = 5,
+    GBSPH_BUF_CELL = 6
+};
+
+/* Stages of one step, in the order `oclFluid3D::compute` enqueues them
+ * (libCL/phys/oclFluid3D.cpp:293-342). Each can be run alone through gbsph_fluid3d_stage;
+ * an integrate hook typically runs the last four itself. */
+enum {
+    GBSPH_STAGE_HASH = 0,               /* clHash */
+    GBSPH_STAGE_SORT = 1,               /* oclRadixSort::compute(cell, index, 0, 24) */
+    GBSPH_STAGE_REORDER = 2,            /* clReorder */
+    GBSPH_STAGE_BOUNDS = 3,             /* fill 0xFFFFFFFF + clFindBounds */
+    GBSPH_STAGE_DENSITY = 4,            /* clCalculateDensity */
+    GBSPH_STAGE_FORCES = 5,             /* clCalculateForces */
+    GBSPH_STAGE_CLIP_BOX = 6,           /* clClipBox */
+    GBSPH_STAGE_INTEGRATE_FORCE = 7,    /* clIntegrateForce */
+    GBSPH_STAGE_GRAVITY = 8,            /* clGravity */
+    GBSPH_STAGE_INTEGRATE_VELOCITY = 9  /* clIntegrateVelocity */
+};
+
+/* Options (gbsph_fluid3d_set_option). */
+enum {
+    GBSPH_OPT_FUSED = 0,      /* 1 (default): fused kernels; 0: one kernel per reference stage */
+    GBSPH_OPT_CUDA_GRAPH = 1, /* 1 (default): replay the step as a captured CUDA graph */
+    GBSPH_OPT_BRICK_WIDTH = 2, /* LINEAR_GRID neighbour bricks: cells per brick along x (1..16) */
+    GBSPH_OPT_PROFILE = 3      /* 1: compute() runs eagerly and records a CUDA event pair per
+                                  stage (the reference's CL_QUEUE_PROFILING_ENABLE events,
+                                  libCL/oclDevice.cpp:31, libCL/oclKernel.cpp:162-202) */
+};
+
+typedef struct gbsph_fluid3d_s* gbsph_fluid3d_t;
+
+/* Called by compute() in place of the clip/integrate stages when set. Replaces
+ * `addEventHandler(srtEvent&)` with `EVT_INTEGRATE` (libCL/phys/oclFluid3D.h:69-70,
+ * libCL/phys/oclFluid3D.cpp:287-291,325-328). Return 0 on success. */
+typedef int (*gbsph_fluid3d_hook_fn)(gbsph_fluid3d_t h, void* stream, void* user);
+
+/* oclFluid3D(oclContext&, oclProgram*) -- libCL/phys/oclFluid3D.cpp:21-83. Allocates
+ * zeroed float4 buffers for the default 256 particles on the current CUDA device. */
+GBSPH_API int gbsph_fluid3d_create(gbsph_fluid3d_t* out);
+/* ~oclFluid3D -- libCL/phys/oclFluid3D.cpp:85-90. Frees owned buffers only. */
+GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h);
+/* compile() -- libCL/phys/oclFluid3D.cpp:273-285: loads the default parameters of
+ * `clInitFluid` (libCL/phys/oclFluid3D.cl:130-148). */
+GBSPH_API int gbsph_fluid3d_compile(gbsph_fluid3d_t h);
+/* setParticleCount -- libCL/phys/oclFluid3D.cpp:92-124. Re-creates owned buffers (contents
+ * are lost, zero-filled). A borrowed buffer smaller than n is an error (it cannot be
+ * resized here). */
+GBSPH_API int gbsph_fluid3d_set_particle_count(gbsph_fluid3d_t h, size_t n);
+/* getParticleCount -- libCL/phys/oclFluid3D.cpp:126-129. */
+GBSPH_API size_t gbsph_fluid3d_get_particle_count(gbsph_fluid3d_t h);
+/* setPositionBuffer / setVelocityBuffer / setForceBuffer -- libCL/phys/oclFluid3D.cpp:131-165.
+ * `device_ptr` is borrowed (never freed). Position needs count == N, velocity/force
+ * count >= N. Only POSITION, VELOCITY and FORCE are settable. */
+GBSPH_API int gbsph_fluid3d_set_buffer(gbsph_fluid3d_t h, int which, void* device_ptr,
+                                       size_t count);
+/* get*Buffer -- libCL/phys/oclFluid3D.cpp:171-201. Returns the device pointer, or NULL. */
+GBSPH_API void* gbsph_fluid3d_get_buffer(gbsph_fluid3d_t h, int which, size_t* count);
+/* getParameters -- libCL/phys/oclFluid3D.cpp:204-207. Host-side struct, read at every
+ * compute(); edit it in place. */
+GBSPH_API gbsph_fluid3d_params* gbsph_fluid3d_get_params(gbsph_fluid3d_t h);
+/* Recomputes kernelConstant, pressureConstant and viscosityConstant from cellSize and
+ * viscosity with the formulas of `clInitFluid` (libCL/phys/oclFluid3D.cl:123-128,145-147)
+ * when dims == 3; when dims == 2 it uses the 2D normalisations of the same kernels
+ * (poly6 4/(pi h^8), spiky gradient 30/(pi h^5), viscosity Laplacian 40/(pi h^5)). */
+GBSPH_API int gbsph_fluid3d_params_derive(gbsph_fluid3d_params* p);
+/* Fills `p` with the defaults compile() loads: `clInitFluid` (libCL/phys/oclFluid3D.cl:130-148)
+ * plus the reference's hard-coded gravity and clip box. Host only; needs no device. */
+GBSPH_API int gbsph_fluid3d_default_params(gbsph_fluid3d_params* p);
+GBSPH_API int gbsph_fluid3d_set_integrate_hook(gbsph_fluid3d_t h, gbsph_fluid3d_hook_fn fn,
+                                               void* user);
+GBSPH_API int gbsph_fluid3d_set_option(gbsph_fluid3d_t h, int option, int value);
+/* compute(oclDevice&) -- libCL/phys/oclFluid3D.cpp:293-342. Asynchronous on `stream`. */
+GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream);
+/* One reference stage alone (GBSPH_STAGE_*), asynchronous on `stream`. */
+GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream);
+/* Copies the cell table out as two uint32 arrays of n_cells entries (device pointers),
+ * 0xFFFFFFFF for empty cells, as `clFindBounds` leaves bfCellStart/bfCellEnd. n_cells is
+ * 262144 in REFERENCE_HASH mode and nx*ny*nz in LINEAR_GRID mode. */
+GBSPH_API int gbsph_fluid3d_get_cell_bounds(gbsph_fluid3d_t h, uint32_t* cell_start,
+                                            uint32_t* cell_end, size_t n_cells, void* stream);
+GBSPH_API int gbsph_fluid3d_sync_status(gbsph_fluid3d_t h, void* stream);
+/* With GBSPH_OPT_PROFILE on: waits for the last profiled compute() and writes the duration
+ * in milliseconds of each of its stages (front end = scratch clear + hash, sort passes incl.
+ * the fused reorder, cell bounds, density, forces + integration) into ms[0..4]. Returns the
+ * number of stages written (5) or a negative status. Replaces oclKernel::getStartTime /
+ * getEndTime (libCL/oclKernel.cpp:167-202). */
+GBSPH_API int gbsph_fluid3d_stage_times(gbsph_fluid3d_t h, float* ms, int max_stages);
+GBSPH_API const char* gbsph_fluid3d_last_error(gbsph_fluid3d_t h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBSPH_H */

@@ -1,0 +1,344 @@
+"""GB300 (sm_103a) SPH fluid step and radix sort: Python mirror of the C ABI in include/gbsph.h.
+
+The classes keep the names and method names of the reference's C++ classes
+(jochenstier/libcl): `RadixSort` <-> `oclRadixSort` (libCL/sort/oclRadixSort.h:22-49),
+`Fluid3D` <-> `oclFluid3D` (libCL/phys/oclFluid3D.h:21-123). Device memory and streams come
+from PyTorch (plumbing only); every computation runs in the CUDA library `libgbsph.so`,
+loaded with ctypes. There is no fallback: if the library is missing, importing the
+bindings raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_lib" / "libgbsph.so"
+
+# status codes (include/gbsph.h)
+OK = 0
+ERR_ARGUMENT = -1
+ERR_SIZE_MISMATCH = -2
+ERR_TOO_LARGE = -3
+ERR_BIT_RANGE = -4
+ERR_CUDA = -5
+ERR_DEVICE_TIMEOUT = -6
+ERR_NOT_COMPILED = -7
+ERR_OUT_OF_MEMORY = -8
+ERR_DEVICE_RANGE = -9
+ERR_STATE = -10
+
+KEY_REFERENCE_HASH = 0
+KEY_LINEAR_GRID = 1
+
+BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY, BUF_INDEX, BUF_CELL = range(7)
+(STAGE_HASH, STAGE_SORT, STAGE_REORDER, STAGE_BOUNDS, STAGE_DENSITY, STAGE_FORCES, STAGE_CLIP_BOX,
+ STAGE_INTEGRATE_FORCE, STAGE_GRAVITY, STAGE_INTEGRATE_VELOCITY) = range(10)
+OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE = range(4)
+STAGE_TIME_NAMES = ("front_end", "sort", "bounds", "density", "forces")
+
+REF_BUCKETS = 262144  # cBucketCount, libCL/phys/oclFluid3D.cpp:17
+
+
+class Fluid3DParams(C.Structure):
+    """gbsph_fluid3d_params: oclFluid3D::Params (libCL/phys/oclFluid3D.h:48-63) + extensions."""
+    _fields_ = [(n, C.c_float) for n in (
+        "deltaTime", "particleRadius", "cellSize", "mass", "viscosity", "pressure", "density",
+        "spacing", "stiffness", "viscosityConstant", "pressureConstant", "kernelConstant",
+        "velocitylimit")] + [
+        ("gravity", C.c_float * 4), ("boxMin", C.c_float * 4), ("boxMax", C.c_float * 4),
+        ("gridOrigin", C.c_float * 4), ("gridDim", C.c_int32 * 4), ("keyMode", C.c_int32),
+        ("dims", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+
+HOOK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
+LOG_FN = C.CFUNCTYPE(None, C.c_int, C.c_char_p, C.c_void_p)
+
+# name -> (restype, argtypes); every symbol declared in include/gbsph.h
+_P, _I, _SZ, _U32P = C.c_void_p, C.c_int, C.c_size_t, C.POINTER(C.c_uint32)
+SIGNATURES = {
+    "gbsph_status_string": (C.c_char_p, [_I]),
+    "gbsph_version": (_I, []),
+    "gbsph_set_logger": (None, [LOG_FN, _P]),
+    "gbsph_radix_sort_create": (_I, [C.POINTER(_P)]),
+    "gbsph_radix_sort_destroy": (_I, [_P]),
+    "gbsph_radix_sort_compute": (_I, [_P, _P, _P, _SZ, _SZ, _I, _I, _P]),
+    "gbsph_radix_sort_cell_bounds": (_I, [_P, _P, _SZ, _P, _P, _SZ, _P]),
+    "gbsph_radix_sort_sync_status": (_I, [_P, _P]),
+    "gbsph_radix_sort_last_error": (C.c_char_p, [_P]),
+    "gbsph_fluid3d_create": (_I, [C.POINTER(_P)]),
+    "gbsph_fluid3d_destroy": (_I, [_P]),
+    "gbsph_fluid3d_compile": (_I, [_P]),
+    "gbsph_fluid3d_set_particle_count": (_I, [_P, _SZ]),
+    "gbsph_fluid3d_get_particle_count": (_SZ, [_P]),
+    "gbsph_fluid3d_set_buffer": (_I, [_P, _I, _P, _SZ]),
+    "gbsph_fluid3d_get_buffer": (_P, [_P, _I, C.POINTER(_SZ)]),
+    "gbsph_fluid3d_get_params": (C.POINTER(Fluid3DParams), [_P]),
+    "gbsph_fluid3d_params_derive": (_I, [C.POINTER(Fluid3DParams)]),
+    "gbsph_fluid3d_default_params": (_I, [C.POINTER(Fluid3DParams)]),
+    "gbsph_fluid3d_set_integrate_hook": (_I, [_P, HOOK_FN, _P]),
+    "gbsph_fluid3d_set_option": (_I, [_P, _I, _I]),
+    "gbsph_fluid3d_compute": (_I, [_P, _P]),
+    "gbsph_fluid3d_stage": (_I, [_P, _I, _P]),
+    "gbsph_fluid3d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
+    "gbsph_fluid3d_sync_status": (_I, [_P, _P]),
+    "gbsph_fluid3d_last_error": (C.c_char_p, [_P]),
+    "gbsph_fluid3d_stage_times": (_I, [_P, C.POINTER(C.c_float), _I]),
+}
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Loads libgbsph.so (building nothing). Raises if it is missing: there is no fallback."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} not found: build it with `python -m libcl_gb300.build`")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class GbsphError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        lib = load_library()
+        super().__init__(f"{lib.gbsph_status_string(status).decode()}: {message}")
+
+
+def status_name(status: int) -> str:
+    return load_library().gbsph_status_string(status).decode()
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else int(t.data_ptr())
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+        return int(torch.cuda.current_stream().cuda_stream)
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class RadixSort:
+    """oclRadixSort: stable LSD sort of uint32 (key, value) pairs in place on key bits
+    [start_bit, end_bit) (libCL/sort/oclRadixSort.cpp:62-144)."""
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_radix_sort_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_radix_sort_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_radix_sort_destroy(self._h)
+            self._h = None
+
+    def last_error(self) -> str:
+        return self._lib.gbsph_radix_sort_last_error(self._h).decode()
+
+    def compute_raw(self, keys, values, start_bit: int, end_bit: int, stream=None) -> int:
+        """Returns the status code (no raise); keys/values are int32/uint32 CUDA tensors."""
+        return self._lib.gbsph_radix_sort_compute(self._h, _ptr(keys), _ptr(values), keys.numel(),
+                                                  values.numel(), start_bit, end_bit, _stream(stream))
+
+    def compute(self, keys, values, start_bit: int = 0, end_bit: int = 32, stream=None) -> None:
+        rc = self.compute_raw(keys, values, start_bit, end_bit, stream)
+        if rc:
+            raise GbsphError(rc, self.last_error())
+
+    def cell_bounds(self, sorted_keys, cell_start, cell_end, stream=None) -> None:
+        rc = self._lib.gbsph_radix_sort_cell_bounds(self._h, _ptr(sorted_keys), sorted_keys.numel(),
+                                                    _ptr(cell_start), _ptr(cell_end), cell_start.numel(),
+                                                    _stream(stream))
+        if rc:
+            raise GbsphError(rc, self.last_error())
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_radix_sort_sync_status(self._h, _stream(stream))
+
+
+class Fluid3D:
+    """oclFluid3D (libCL/phys/oclFluid3D.h:21-123): construct, compile(), set buffers,
+    compute(), read position/velocity and the sorted buffers (.w = density / pressure)."""
+
+    EVT_INTEGRATE = "OnIntegrate"
+    cLocalSize = 256
+    cBucketCount = REF_BUCKETS
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_fluid3d_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_fluid3d_create")
+        self._h = h
+        self._hook = None
+        self._borrowed = {}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_fluid3d_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_fluid3d_last_error(self._h).decode())
+
+    def last_error(self) -> str:
+        return self._lib.gbsph_fluid3d_last_error(self._h).decode()
+
+    def compile(self) -> None:
+        self._check(self._lib.gbsph_fluid3d_compile(self._h))
+
+    def compute(self, stream=None) -> None:
+        self._check(self._lib.gbsph_fluid3d_compute(self._h, _stream(stream)))
+
+    def compute_raw(self, stream=None) -> int:
+        return self._lib.gbsph_fluid3d_compute(self._h, _stream(stream))
+
+    def stage(self, stage: int, stream=None) -> None:
+        self._check(self._lib.gbsph_fluid3d_stage(self._h, stage, _stream(stream)))
+
+    def setParticleCount(self, n: int) -> None:
+        self._check(self._lib.gbsph_fluid3d_set_particle_count(self._h, n))
+
+    def getParticleCount(self) -> int:
+        return int(self._lib.gbsph_fluid3d_get_particle_count(self._h))
+
+    def getParameters(self) -> Fluid3DParams:
+        return self._lib.gbsph_fluid3d_get_params(self._h).contents
+
+    def set_option(self, option: int, value: int) -> None:
+        self._check(self._lib.gbsph_fluid3d_set_option(self._h, option, value))
+
+    def _set(self, which: int, tensor) -> int:
+        rc = self._lib.gbsph_fluid3d_set_buffer(self._h, which, _ptr(tensor), tensor.numel() // 4)
+        if rc == 0:
+            self._borrowed[which] = tensor  # keep the borrowed memory alive
+        return rc
+
+    def setPositionBuffer(self, t) -> None:
+        self._check(self._set(BUF_POSITION, t))
+
+    def setVelocityBuffer(self, t) -> None:
+        self._check(self._set(BUF_VELOCITY, t))
+
+    def setForceBuffer(self, t) -> None:
+        self._check(self._set(BUF_FORCE, t))
+
+    def buffer(self, which: int):
+        """A torch view of one of the library's device buffers (no copy)."""
+        import torch
+        count = C.c_size_t()
+        p = self._lib.gbsph_fluid3d_get_buffer(self._h, which, C.byref(count))
+        if not p:
+            raise GbsphError(ERR_ARGUMENT, f"no buffer {which}")
+        if which in self._borrowed:
+            return self._borrowed[which]
+        n = count.value
+        is_f4 = which in (BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY)
+        return _device_view(p, n * 4 if is_f4 else n, torch.float32 if is_f4 else torch.int32,
+                            (n, 4) if is_f4 else (n,))
+
+    def getPositionBuffer(self):
+        return self.buffer(BUF_POSITION)
+
+    def getVelocityBuffer(self):
+        return self.buffer(BUF_VELOCITY)
+
+    def getForceBuffer(self):
+        return self.buffer(BUF_FORCE)
+
+    def getSortedPositionBuffer(self):
+        return self.buffer(BUF_SORTED_POSITION)
+
+    def getSortedVelocityBuffer(self):
+        return self.buffer(BUF_SORTED_VELOCITY)
+
+    def getIndexBuffer(self):
+        return self.buffer(BUF_INDEX)
+
+    def getCellBuffer(self):
+        return self.buffer(BUF_CELL)
+
+    def cell_bounds(self, n_cells: int, stream=None):
+        import torch
+        cs = torch.empty(n_cells, dtype=torch.int32, device="cuda")
+        ce = torch.empty(n_cells, dtype=torch.int32, device="cuda")
+        self._check(self._lib.gbsph_fluid3d_get_cell_bounds(self._h, _ptr(cs), _ptr(ce), n_cells, _stream(stream)))
+        return cs, ce
+
+    def addEventHandler(self, fn) -> None:
+        """EVT_INTEGRATE hook: fn(fluid, stream_handle) runs in place of the clip/integrate
+        stages (libCL/phys/oclFluid3D.cpp:287-291,325-328); return 0 on success."""
+        if fn is None:
+            self._hook = None
+            self._check(self._lib.gbsph_fluid3d_set_integrate_hook(self._h, HOOK_FN(), None))
+            return
+
+        def tramp(_h, stream, _user):
+            try:
+                return int(fn(self, stream) or 0)
+            except Exception:  # an exception must not unwind through C
+                return -1
+
+        self._hook = HOOK_FN(tramp)
+        self._check(self._lib.gbsph_fluid3d_set_integrate_hook(self._h, self._hook, None))
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_fluid3d_sync_status(self._h, _stream(stream))
+
+    def stage_times(self) -> dict:
+        """Per-stage milliseconds of the last compute() run with OPT_PROFILE on."""
+        buf = (C.c_float * 5)()
+        n = self._lib.gbsph_fluid3d_stage_times(self._h, buf, 5)
+        if n < 0:
+            raise GbsphError(n, self.last_error())
+        return {STAGE_TIME_NAMES[i]: float(buf[i]) for i in range(n)}
+
+
+def params_derive(p: Fluid3DParams) -> None:
+    rc = load_library().gbsph_fluid3d_params_derive(C.byref(p))
+    if rc:
+        raise GbsphError(rc, "params_derive")
+
+
+def default_params() -> Fluid3DParams:
+    """The parameters compile() loads (clInitFluid, libCL/phys/oclFluid3D.cl:130-148)."""
+    p = Fluid3DParams()
+    rc = load_library().gbsph_fluid3d_default_params(C.byref(p))
+    if rc:
+        raise GbsphError(rc, "default_params")
+    return p
+
+
+class _CudaArrayView:
+    """Minimal __cuda_array_interface__ provider to wrap library-owned device memory."""
+
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr,
+                                         "data": (int(ptr), False), "version": 3, "strides": None}
+
+
+def _device_view(ptr: int, numel: int, dtype, shape):
+    import torch
+    typestr = "<f4" if dtype == torch.float32 else "<i4"
+    return torch.as_tensor(_CudaArrayView(ptr, shape, typestr), device="cuda")

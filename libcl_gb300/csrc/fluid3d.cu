@@ -1,0 +1,755 @@
+// fluid3d.cu -- host side of the 3D SPH fluid: the oclFluid3D replacement behind the C ABI.
+//
+// One step (libCL/phys/oclFluid3D.cpp:293-342) is enqueued on the caller's stream as:
+//   memset(sort scratch) -> k_hash (+digit histogram, +sparse clear of last step's cells)
+//   -> one-sweep passes (last pass gathers sorted position/velocity = clReorder)
+//   -> cell bounds (+ occupied-brick list) -> density -> forces (+clip/integrate/gravity)
+// and, once the cell table is in steady state, replayed as a captured CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fluid3d_kernels.cuh"
+
+using namespace gbsph;
+
+namespace {
+
+constexpr uint32_t BRICK_CAP = 2048;  // staged candidates per brick (float4 per array)
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t count = 0;
+    bool owned = false;
+};
+
+float bits_to_float(uint32_t b) {
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// Smallest float x >= 0 with sqrtf(x) >= h. sqrtf is correctly rounded and monotone, so for
+// every float r2 >= 0: (sqrtf(r2) < h) == (r2 < threshold).
+float r2_threshold(float h) {
+    if (!(h > 0.0f) || std::isinf(h)) return 0.0f;
+    uint32_t lo = 0, hi = 0x7f800000u;  // sqrtf(+0) = 0 < h, sqrtf(inf) = inf >= h
+    while (hi - lo > 1) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (std::sqrt(bits_to_float(mid)) >= h) hi = mid;
+        else lo = mid;
+    }
+    return bits_to_float(hi);
+}
+
+int bits_for(uint64_t cells) {  // number of key bits to sort so that every key < cells is covered
+    int b = 0;
+    while (b < 32 && (1ull << b) < cells) b++;
+    return std::max(b, 1);
+}
+
+}  // namespace
+
+struct gbsph_fluid3d_s {
+    int device = 0;
+    gbsph_fluid3d_params params{};
+    bool compiled = false;
+    size_t n = 256;
+    DevBuf buf[3];  // position, velocity, force
+    size_t n_alloc = 0;
+    void* pblock = nullptr;  // per-particle internal arrays
+    float4* spos = nullptr;
+    float4* svel = nullptr;
+    uint32_t *keys_a = nullptr, *keys_b = nullptr, *keys_c = nullptr;
+    uint32_t *vals_a = nullptr, *vals_b = nullptr, *index = nullptr, *bricks = nullptr;
+    uint32_t* hash_tables = nullptr;  // cell start / end, REF_BUCKETS each
+    uint2* table = nullptr;           // LINEAR_GRID interleaved table
+    size_t table_cells = 0;
+    bool table_clean = false;  // table empty except the runs of keys_c
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t* err = nullptr;
+    gbsph_fluid3d_hook_fn hook = nullptr;
+    void* hook_user = nullptr;
+    int opt_fused = 1, opt_graph = 1, opt_bw = 8, opt_profile = 0;
+    cudaEvent_t ev[6] = {};
+    bool ev_valid = false;
+    int dens_blocks = 0, force_blocks = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<char> gkey;
+    std::string last_error;
+};
+
+namespace {
+
+using H = gbsph_fluid3d_s;
+
+void default_params(gbsph_fluid3d_params* p) {
+    // clInitFluid, libCL/phys/oclFluid3D.cl:130-148 (double literals evaluated in double)
+    std::memset(p, 0, sizeof(*p));
+    p->deltaTime = (float)0.005;
+    p->mass = (float)0.006;
+    p->density = 1000;
+    p->viscosity = (float)6.0;
+    p->pressure = 0;
+    p->velocitylimit = 500;
+    p->stiffness = 1;
+    p->spacing = (float)(0.87 * (double)std::pow(p->mass / p->density, 1 / 3.0f));
+    p->particleRadius = (float)(0.5 * (double)p->spacing);
+    p->cellSize = (float)(2.0 * (double)p->spacing);
+    p->dims = 3;
+    gbsph_fluid3d_params_derive(p);
+    // hard-coded kernel arguments, libCL/phys/oclFluid3D.cpp:256-268
+    p->gravity[0] = -9.8f * 0.0f;
+    p->gravity[1] = -9.8f * 0.0f;
+    p->gravity[2] = -9.8f * 1.0f;
+    p->gravity[3] = -9.8f * 0.0f;
+    for (int i = 0; i < 3; i++) {
+        p->boxMin[i] = -1.0f;
+        p->boxMax[i] = 1.0f;
+    }
+    p->keyMode = GBSPH_KEY_REFERENCE_HASH;
+}
+
+bool finite_all(const float* v, int n) {
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+int validate_params(H* h) {
+    const gbsph_fluid3d_params& p = h->params;
+    if (!finite_all(&p.deltaTime, 13) || !finite_all(p.gravity, 4) || !std::isfinite(p.boxMin[0]) ||
+        !std::isfinite(p.boxMin[1]) || !std::isfinite(p.boxMax[0]) || !std::isfinite(p.boxMax[1]) ||
+        !finite_all(p.gridOrigin, 3))
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "parameters hold a NaN or infinity");
+    if (!(p.cellSize > 0.0f)) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "cellSize must be > 0");
+    if (p.dims != 2 && p.dims != 3) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "dims must be 2 or 3");
+    if (p.keyMode == GBSPH_KEY_LINEAR_GRID) {
+        const int64_t nz = p.dims == 2 ? 1 : p.gridDim[2];
+        if (p.gridDim[0] < 1 || p.gridDim[1] < 1 || nz < 1)
+            return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "gridDim must be positive");
+        if ((int64_t)p.gridDim[0] * p.gridDim[1] * nz > (1ll << 30))
+            return fail(&h->last_error, GBSPH_ERR_TOO_LARGE, "grid has more than 2^30 cells");
+    } else if (p.keyMode != GBSPH_KEY_REFERENCE_HASH) {
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown keyMode");
+    }
+    return GBSPH_OK;
+}
+
+KParams make_kparams(const H* h) {
+    const gbsph_fluid3d_params& p = h->params;
+    KParams k;
+    std::memset(&k, 0, sizeof(k));  // padding too: the struct is compared bytewise as a graph key
+    k.dt = p.deltaTime;
+    k.radius = p.particleRadius;
+    k.h = p.cellSize;
+    k.mass = p.mass;
+    k.p0 = p.pressure;
+    k.rho0 = p.density;
+    k.stiff = p.stiffness;
+    k.cvisc = p.viscosityConstant;
+    k.cpress = p.pressureConstant;
+    k.kconst = p.kernelConstant;
+    k.vlimit = p.velocitylimit;
+    k.h2 = p.cellSize * p.cellSize;
+    k.r2_thresh = r2_threshold(p.cellSize);
+    k.gravity = make_float4(p.gravity[0], p.gravity[1], p.gravity[2], p.gravity[3]);
+    k.box_min = make_float4(p.boxMin[0], p.boxMin[1], p.boxMin[2], p.boxMin[3]);
+    k.box_max = make_float4(p.boxMax[0], p.boxMax[1], p.boxMax[2], p.boxMax[3]);
+    k.origin = make_float4(p.gridOrigin[0], p.gridOrigin[1], p.gridOrigin[2], 0.0f);
+    k.key_mode = p.keyMode;
+    k.dims = p.dims;
+    if (p.keyMode == GBSPH_KEY_LINEAR_GRID) {
+        k.nx = p.gridDim[0];
+        k.ny = p.gridDim[1];
+        k.nz = p.dims == 2 ? 1 : p.gridDim[2];
+        k.table_cells = (uint32_t)((uint64_t)k.nx * k.ny * k.nz);
+        k.end_bit = bits_for(k.table_cells);
+    } else {
+        k.nx = k.ny = k.nz = 0;
+        k.table_cells = REF_BUCKETS;
+        k.end_bit = 18;  // keys < 2^18; the reference sorts bits [0, 24) of the same keys
+    }
+    k.bw = h->opt_bw;
+    k.bxn = k.nx > 0 ? (k.nx + k.bw - 1) / k.bw : 0;
+    k.n = (uint32_t)h->n;
+    return k;
+}
+
+void invalidate_graph(H* h) {
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+    h->gkey.clear();
+}
+
+void free_particle_arrays(H* h) {
+    if (h->pblock) cudaFree(h->pblock);
+    h->pblock = nullptr;
+    if (h->scratch) cudaFree(h->scratch);
+    h->scratch = nullptr;
+    h->n_alloc = 0;
+}
+
+int alloc_particle_arrays(H* h, size_t n) {
+    free_particle_arrays(h);
+    const size_t n4 = (n + 63) & ~size_t(63);
+    const size_t bytes = n4 * (2 * 16 + 7 * 4);
+    GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->pblock, bytes));
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->pblock, 0, bytes));
+    char* p = (char*)h->pblock;
+    h->spos = (float4*)p;
+    p += n4 * 16;
+    h->svel = (float4*)p;
+    p += n4 * 16;
+    uint32_t** arr[7] = {&h->keys_a, &h->keys_b, &h->keys_c, &h->vals_a, &h->vals_b, &h->index, &h->bricks};
+    for (auto a : arr) {
+        *a = (uint32_t*)p;
+        p += n4 * 4;
+    }
+    h->scratch_bytes = onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES);
+    GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, h->scratch_bytes));
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->scratch, 0, h->scratch_bytes));
+    h->n_alloc = n;
+    h->table_clean = false;
+    return GBSPH_OK;
+}
+
+int alloc_owned(H* h, int which, size_t n) {
+    DevBuf& b = h->buf[which];
+    if (b.owned && b.ptr) cudaFree(b.ptr);
+    b = DevBuf();
+    GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&b.ptr, std::max<size_t>(n, 1) * 16));
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemset(b.ptr, 0, std::max<size_t>(n, 1) * 16));
+    b.count = n;
+    b.owned = true;
+    return GBSPH_OK;
+}
+
+// Makes the cell tables match the current parameters.
+int ensure_tables(H* h) {
+    if (h->params.keyMode == GBSPH_KEY_LINEAR_GRID) {
+        const size_t cells = (size_t)h->params.gridDim[0] * h->params.gridDim[1] *
+                             (size_t)(h->params.dims == 2 ? 1 : h->params.gridDim[2]);
+        if (cells != h->table_cells || !h->table) {
+            if (h->table) cudaFree(h->table);
+            h->table = nullptr;
+            h->table_cells = 0;
+            GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->table, cells * sizeof(uint2)));
+            h->table_cells = cells;
+            h->table_clean = false;
+            invalidate_graph(h);
+        }
+    } else if (!h->hash_tables) {
+        GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->hash_tables, 2 * (size_t)REF_BUCKETS * 4));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->hash_tables, 0xFF, 2 * (size_t)REF_BUCKETS * 4));
+    }
+    return GBSPH_OK;
+}
+
+uint32_t* counters(H* h) { return (uint32_t*)((char*)h->scratch + SORT_USER_COUNTER_OFFSET); }
+float4* P4(H* h, int w) { return (float4*)h->buf[w].ptr; }
+
+int grid1(uint32_t n) { return (int)((n + 255) / 256); }
+
+// ---- stage launchers ----------------------------------------------------------------------
+
+int st_hash(H* h, const KParams& kp, cudaStream_t s, bool clear) {
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_prepare(h->scratch, kp.n, sort_passes(0, kp.end_bit), s));
+    const int blocks = std::max(1, std::min(grid1(kp.n), num_sms() * 8));
+    if (clear)
+        k_hash<true><<<blocks, 256, 0, s>>>(P4(h, 0), kp, h->keys_a, (uint32_t*)h->scratch, h->keys_c, h->table);
+    else
+        k_hash<false><<<blocks, 256, 0, s>>>(P4(h, 0), kp, h->keys_a, (uint32_t*)h->scratch, nullptr, nullptr);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather) {
+    OnesweepArgs a;
+    a.keys_in = h->keys_a;
+    a.vals_in = nullptr;
+    a.keys_out = h->keys_c;
+    a.vals_out = h->index;
+    a.tmp_keys[0] = h->keys_b;
+    a.tmp_vals[0] = h->vals_b;
+    a.tmp_keys[1] = h->keys_a;
+    a.tmp_vals[1] = h->vals_a;
+    a.n = kp.n;
+    a.start_bit = 0;
+    a.end_bit = kp.end_bit;
+    a.scratch = h->scratch;
+    a.err = h->err;
+    if (gather) {
+        a.gather.n_gather = 2;
+        a.gather.src[0] = P4(h, 0);
+        a.gather.src[1] = P4(h, 1);
+        a.gather.dst[0] = h->spos;
+        a.gather.dst[1] = h->svel;
+    }
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
+    return GBSPH_OK;
+}
+
+int st_reorder(H* h, const KParams& kp, cudaStream_t s) {
+    k_reorder<<<grid1(kp.n), 256, 0, s>>>(h->index, P4(h, 0), P4(h, 1), h->spos, h->svel, kp.n);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_bounds(H* h, const KParams& kp, cudaStream_t s, bool full_clear) {
+    if (kp.key_mode == GBSPH_KEY_LINEAR_GRID) {
+        if (full_clear) GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->table_cells * sizeof(uint2), s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(counters(h), 0, 16, s));
+        k_bounds_linear<<<grid1(kp.n), 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
+        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    } else {
+        GBSPH_CUDA_TRY(&h->last_error, cell_bounds_launch(h->keys_c, kp.n, h->hash_tables,
+                                                          h->hash_tables + REF_BUCKETS, REF_BUCKETS, h->err, s));
+    }
+    return GBSPH_OK;
+}
+
+int st_density_exact(H* h, const KParams& kp, cudaStream_t s) {
+    if (kp.key_mode == GBSPH_KEY_LINEAR_GRID)
+        k_density_exact<GBSPH_KEY_LINEAR_GRID><<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, PairTable{h->table}, kp);
+    else
+        k_density_exact<GBSPH_KEY_REFERENCE_HASH><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_forces_exact(H* h, const KParams& kp, cudaStream_t s) {
+    if (kp.key_mode == GBSPH_KEY_LINEAR_GRID)
+        k_forces_exact<GBSPH_KEY_LINEAR_GRID><<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, P4(h, 2), h->index,
+                                                                           PairTable{h->table}, kp);
+    else
+        k_forces_exact<GBSPH_KEY_REFERENCE_HASH><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, P4(h, 2), h->index, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
+    const size_t smem = (size_t)BRICK_CAP * 16;
+    if (kp.dims == 2)
+        k_density_brick<2><<<h->dens_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
+    else
+        k_density_brick<3><<<h->dens_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_force_brick(H* h, const KParams& kp, cudaStream_t s, bool fused) {
+    const size_t smem = (size_t)BRICK_CAP * 32;
+    auto launch = [&](auto kern) {
+        kern<<<h->force_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2),
+                                                          h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
+    };
+    if (kp.dims == 2) {
+        if (fused) launch(k_force_brick<2, true>);
+        else launch(k_force_brick<2, false>);
+    } else {
+        if (fused) launch(k_force_brick<3, true>);
+        else launch(k_force_brick<3, false>);
+    }
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int st_post(H* h, const KParams& kp, int stage, cudaStream_t s) {
+    const int g = grid1(kp.n);
+    switch (stage) {
+        case GBSPH_STAGE_CLIP_BOX: k_clip_box<<<g, 256, 0, s>>>(h->spos, h->svel, P4(h, 2), h->index, kp); break;
+        case GBSPH_STAGE_INTEGRATE_FORCE: k_integrate_force<<<g, 256, 0, s>>>(P4(h, 1), P4(h, 2), kp); break;
+        case GBSPH_STAGE_GRAVITY: k_gravity<<<g, 256, 0, s>>>(P4(h, 2), kp); break;
+        case GBSPH_STAGE_INTEGRATE_VELOCITY: k_integrate_velocity<<<g, 256, 0, s>>>(P4(h, 0), P4(h, 1), kp); break;
+        default: return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "not a post stage");
+    }
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+int run_hook(H* h, cudaStream_t s) {
+    const int rc = h->hook(h, (void*)s, h->hook_user);
+    if (rc != 0) return fail(&h->last_error, GBSPH_ERR_STATE, "integrate hook returned " + std::to_string(rc));
+    return GBSPH_OK;
+}
+
+#define RC(x)                   \
+    do {                        \
+        int _rc = (x);          \
+        if (_rc) return _rc;    \
+    } while (0)
+
+// The reference's kernel sequence, one kernel per stage (GBSPH_OPT_FUSED = 0).
+int enqueue_staged(H* h, const KParams& kp, cudaStream_t s) {
+    h->table_clean = false;
+    RC(st_hash(h, kp, s, false));
+    RC(st_sort(h, kp, s, false));
+    RC(st_reorder(h, kp, s));
+    RC(st_bounds(h, kp, s, true));
+    RC(st_density_exact(h, kp, s));
+    RC(st_forces_exact(h, kp, s));
+    if (h->hook) return run_hook(h, s);
+    for (int st = GBSPH_STAGE_CLIP_BOX; st <= GBSPH_STAGE_INTEGRATE_VELOCITY; ++st) RC(st_post(h, kp, st, s));
+    return GBSPH_OK;
+}
+
+int mark(H* h, int i, cudaStream_t s) {
+    if (!h->opt_profile) return GBSPH_OK;
+    if (!h->ev[i]) GBSPH_CUDA_TRY(&h->last_error, cudaEventCreate(&h->ev[i]));
+    GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->ev[i], s));
+    return GBSPH_OK;
+}
+
+// The fused step (default).
+int enqueue_fused(H* h, const KParams& kp, cudaStream_t s) {
+    const bool linear = kp.key_mode == GBSPH_KEY_LINEAR_GRID;
+    const bool clear = linear && h->table_clean;
+    h->ev_valid = false;
+    RC(mark(h, 0, s));
+    if (linear && !h->table_clean)
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->table_cells * sizeof(uint2), s));
+    h->table_clean = false;
+    RC(st_hash(h, kp, s, clear));
+    RC(mark(h, 1, s));
+    RC(st_sort(h, kp, s, true));
+    RC(mark(h, 2, s));
+    if (linear) {
+        // counters were zeroed with the sort scratch in st_hash
+        k_bounds_linear<<<grid1(kp.n), 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
+        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+        h->table_clean = true;
+        RC(mark(h, 3, s));
+        RC(st_density_brick(h, kp, s));
+        RC(mark(h, 4, s));
+        RC(st_force_brick(h, kp, s, h->hook == nullptr));
+    } else {
+        RC(st_bounds(h, kp, s, true));
+        RC(mark(h, 3, s));
+        RC(st_density_exact(h, kp, s));
+        RC(mark(h, 4, s));
+        RC(st_forces_exact(h, kp, s));
+        if (!h->hook) {
+            k_post_fused<<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2), kp);
+            GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+        }
+    }
+    RC(mark(h, 5, s));
+    h->ev_valid = h->opt_profile != 0;
+    if (h->hook) return run_hook(h, s);
+    return GBSPH_OK;
+}
+
+std::vector<char> graph_key(const H* h, const KParams& kp) {
+    std::vector<char> k(sizeof(KParams) + 3 * sizeof(void*) + 4 * sizeof(int));
+    char* p = k.data();
+    std::memcpy(p, &kp, sizeof(KParams));
+    p += sizeof(KParams);
+    for (int i = 0; i < 3; i++) {
+        std::memcpy(p, &h->buf[i].ptr, sizeof(void*));
+        p += sizeof(void*);
+    }
+    int o[4] = {h->opt_fused, h->opt_bw, (int)h->table_cells, h->dens_blocks};
+    std::memcpy(p, o, sizeof(o));
+    return k;
+}
+
+int setup_kernels(H* h) {
+    const int sms = num_sms();
+    int nb = 0;
+    const size_t dsm = (size_t)BRICK_CAP * 16, fsm = (size_t)BRICK_CAP * 32;
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_brick<3>, BRICK_THREADS, dsm));
+    h->dens_blocks = std::max(1, nb) * sms;
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true>, BRICK_THREADS, fsm));
+    h->force_blocks = std::max(1, nb) * sms;
+    return GBSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GBSPH_API int gbsph_fluid3d_params_derive(gbsph_fluid3d_params* p) {
+    if (!p) return GBSPH_ERR_ARGUMENT;
+    const double pi = (double)(float)M_PI;
+    const double h = p->cellSize;
+    if (p->dims == 2) {
+        p->kernelConstant = (float)(4.0 / (pi * std::pow(h, 8.0)));
+        p->pressureConstant = (float)(30.0 / (pi * std::pow(h, 5.0)));
+        p->viscosityConstant = (float)((double)p->viscosity * 40.0 / (pi * std::pow(h, 5.0)));
+    } else {
+        // DensityConstant / PressureConstant / ViscosityConstant, libCL/phys/oclFluid3D.cl:123-128
+        p->kernelConstant = (float)(315.0 / (64.0 * pi * (double)std::pow(p->cellSize, 9.0f)));
+        p->viscosityConstant = (float)(-(double)p->viscosity * (-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
+        p->pressureConstant = (float)(-(-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
+    }
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_default_params(gbsph_fluid3d_params* p) {
+    if (!p) return GBSPH_ERR_ARGUMENT;
+    default_params(p);
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_create(gbsph_fluid3d_t* out) {
+    if (!out) return GBSPH_ERR_ARGUMENT;
+    *out = nullptr;
+    H* h = new H();
+    int rc = GBSPH_OK;
+    if (cudaGetDevice(&h->device) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc && cudaMalloc(&h->err, 256) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc && cudaMemset(h->err, 0, 256) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc) rc = alloc_particle_arrays(h, h->n);
+    for (int w = 0; w < 3 && !rc; w++) rc = alloc_owned(h, w, h->n);
+    if (rc) {
+        cudaGetLastError();
+        gbsph_fluid3d_destroy(h);
+        return rc;
+    }
+    default_params(&h->params);
+    *out = h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    cudaSetDevice(h->device);
+    invalidate_graph(h);
+    for (auto& b : h->buf)
+        if (b.owned && b.ptr) cudaFree(b.ptr);
+    free_particle_arrays(h);
+    if (h->hash_tables) cudaFree(h->hash_tables);
+    if (h->table) cudaFree(h->table);
+    if (h->err) cudaFree(h->err);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    for (auto e : h->ev)
+        if (e) cudaEventDestroy(e);
+    delete h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_compile(gbsph_fluid3d_t h) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    default_params(&h->params);
+    RC(setup_kernels(h));
+    h->compiled = true;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_set_particle_count(gbsph_fluid3d_t h, size_t n) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (n == 0) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "particle count must be > 0");
+    if (n > SORT_MAX_KEYS - SORT_TILE)
+        return fail(&h->last_error, GBSPH_ERR_TOO_LARGE, "particle count above " + std::to_string(SORT_MAX_KEYS - SORT_TILE));
+    for (int w = 0; w < 3; w++)
+        if (!h->buf[w].owned && h->buf[w].count < n)
+            return fail(&h->last_error, GBSPH_ERR_SIZE_MISMATCH,
+                        "borrowed buffer " + std::to_string(w) + " holds fewer than " + std::to_string(n) + " float4");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    invalidate_graph(h);
+    h->n = n;
+    RC(alloc_particle_arrays(h, n));
+    for (int w = 0; w < 3; w++)
+        if (h->buf[w].owned) RC(alloc_owned(h, w, n));
+    return GBSPH_OK;
+}
+
+GBSPH_API size_t gbsph_fluid3d_get_particle_count(gbsph_fluid3d_t h) { return h ? h->n : 0; }
+
+GBSPH_API int gbsph_fluid3d_set_buffer(gbsph_fluid3d_t h, int which, void* device_ptr, size_t count) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (which < GBSPH_BUF_POSITION || which > GBSPH_BUF_FORCE)
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "only position, velocity and force buffers can be set");
+    if (!device_ptr) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null buffer");
+    if ((uintptr_t)device_ptr % 16 != 0) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "buffer not 16-byte aligned");
+    if (which == GBSPH_BUF_POSITION ? count != h->n : count < h->n)
+        return fail(&h->last_error, GBSPH_ERR_SIZE_MISMATCH,
+                    "buffer holds " + std::to_string(count) + " float4, particle count is " + std::to_string(h->n));
+    DevBuf& b = h->buf[which];
+    if (b.owned && b.ptr) {
+        cudaSetDevice(h->device);
+        cudaFree(b.ptr);
+    }
+    b.ptr = device_ptr;
+    b.count = count;
+    b.owned = false;
+    invalidate_graph(h);
+    return GBSPH_OK;
+}
+
+GBSPH_API void* gbsph_fluid3d_get_buffer(gbsph_fluid3d_t h, int which, size_t* count) {
+    if (!h) return nullptr;
+    void* p = nullptr;
+    switch (which) {
+        case GBSPH_BUF_POSITION:
+        case GBSPH_BUF_VELOCITY:
+        case GBSPH_BUF_FORCE:
+            if (count) *count = h->buf[which].count;
+            return h->buf[which].ptr;
+        case GBSPH_BUF_SORTED_POSITION: p = h->spos; break;
+        case GBSPH_BUF_SORTED_VELOCITY: p = h->svel; break;
+        case GBSPH_BUF_INDEX: p = h->index; break;
+        case GBSPH_BUF_CELL: p = h->keys_c; break;
+        default: return nullptr;
+    }
+    if (count) *count = h->n;
+    return p;
+}
+
+GBSPH_API gbsph_fluid3d_params* gbsph_fluid3d_get_params(gbsph_fluid3d_t h) { return h ? &h->params : nullptr; }
+
+GBSPH_API int gbsph_fluid3d_set_integrate_hook(gbsph_fluid3d_t h, gbsph_fluid3d_hook_fn fn, void* user) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    h->hook = fn;
+    h->hook_user = user;
+    invalidate_graph(h);
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_set_option(gbsph_fluid3d_t h, int option, int value) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    switch (option) {
+        case GBSPH_OPT_FUSED: h->opt_fused = value ? 1 : 0; break;
+        case GBSPH_OPT_CUDA_GRAPH: h->opt_graph = value ? 1 : 0; break;
+        case GBSPH_OPT_BRICK_WIDTH:
+            if (value < 1 || value > BRICK_W_MAX)
+                return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "brick width must be in [1, 16]");
+            h->opt_bw = value;
+            break;
+        case GBSPH_OPT_PROFILE: h->opt_profile = value ? 1 : 0; break;
+        default: return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown option");
+    }
+    invalidate_graph(h);
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_stage_times(gbsph_fluid3d_t h, float* ms, int max_stages) {
+    if (!h || !ms) return GBSPH_ERR_ARGUMENT;
+    if (!h->ev_valid) return fail(&h->last_error, GBSPH_ERR_STATE, "no profiled compute() recorded");
+    GBSPH_CUDA_TRY(&h->last_error, cudaEventSynchronize(h->ev[5]));
+    const int n = std::min(max_stages, 5);
+    for (int i = 0; i < n; i++) GBSPH_CUDA_TRY(&h->last_error, cudaEventElapsedTime(&ms[i], h->ev[i], h->ev[i + 1]));
+    return n;
+}
+
+GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "compute() before compile()");
+    RC(validate_params(h));
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    RC(ensure_tables(h));
+    const KParams kp = make_kparams(h);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!h->opt_fused) return enqueue_staged(h, kp, s);
+    const bool steady = kp.key_mode != GBSPH_KEY_LINEAR_GRID || h->table_clean;
+    if (h->hook || !h->opt_graph || !steady || h->opt_profile) {
+        const int rc = enqueue_fused(h, kp, s);
+        if (rc) h->table_clean = false;
+        return rc;
+    }
+    std::vector<char> key = graph_key(h, kp);
+    if (!h->gexec || key != h->gkey) {
+        invalidate_graph(h);
+        GBSPH_CUDA_TRY(&h->last_error, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_fused(h, kp, h->cap_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
+        if (rc || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            h->table_clean = false;
+            return rc ? rc : fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            h->gexec = nullptr;
+            h->table_clean = false;
+            return fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        }
+        h->gkey = key;
+    }
+    const cudaError_t le = cudaGraphLaunch(h->gexec, s);
+    if (le != cudaSuccess) {
+        h->table_clean = false;
+        return fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(le));
+    }
+    h->table_clean = true;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "stage before compile()");
+    RC(validate_params(h));
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    RC(ensure_tables(h));
+    const KParams kp = make_kparams(h);
+    cudaStream_t s = (cudaStream_t)stream;
+    h->table_clean = false;
+    switch (stage) {
+        case GBSPH_STAGE_HASH: return st_hash(h, kp, s, false);
+        case GBSPH_STAGE_SORT: return st_sort(h, kp, s, false);
+        case GBSPH_STAGE_REORDER: return st_reorder(h, kp, s);
+        case GBSPH_STAGE_BOUNDS: return st_bounds(h, kp, s, true);
+        case GBSPH_STAGE_DENSITY: return st_density_exact(h, kp, s);
+        case GBSPH_STAGE_FORCES: return st_forces_exact(h, kp, s);
+        case GBSPH_STAGE_CLIP_BOX:
+        case GBSPH_STAGE_INTEGRATE_FORCE:
+        case GBSPH_STAGE_GRAVITY:
+        case GBSPH_STAGE_INTEGRATE_VELOCITY: return st_post(h, kp, stage, s);
+        default: return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown stage");
+    }
+}
+
+GBSPH_API int gbsph_fluid3d_get_cell_bounds(gbsph_fluid3d_t h, uint32_t* cell_start, uint32_t* cell_end,
+                                            size_t n_cells, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!cell_start || !cell_end) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null pointer");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    if (h->params.keyMode == GBSPH_KEY_LINEAR_GRID) {
+        if (n_cells != h->table_cells || !h->table)
+            return fail(&h->last_error, GBSPH_ERR_SIZE_MISMATCH, "n_cells must equal the grid's cell count");
+        k_table_split<<<(unsigned)((n_cells + 255) / 256), 256, 0, s>>>(h->table, (uint32_t)n_cells, cell_start, cell_end);
+        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    } else {
+        if (n_cells != REF_BUCKETS || !h->hash_tables)
+            return fail(&h->last_error, GBSPH_ERR_SIZE_MISMATCH, "n_cells must be 262144");
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(cell_start, h->hash_tables, REF_BUCKETS * 4ull, cudaMemcpyDeviceToDevice, s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(cell_end, h->hash_tables + REF_BUCKETS, REF_BUCKETS * 4ull, cudaMemcpyDeviceToDevice, s));
+    }
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid3d_sync_status(gbsph_fluid3d_t h, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t bits = 0;
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemcpy(&bits, h->err, 4, cudaMemcpyDeviceToHost));
+    if (bits) {
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->err, 0, 4));
+        h->table_clean = false;
+        return fail(&h->last_error, dev_err_to_status(bits), "device error word 0x" + std::to_string(bits));
+    }
+    return GBSPH_OK;
+}
+
+GBSPH_API const char* gbsph_fluid3d_last_error(gbsph_fluid3d_t h) { return h ? h->last_error.c_str() : "null handle"; }
+
+}  // extern "C"

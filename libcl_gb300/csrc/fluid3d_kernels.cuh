@@ -1,0 +1,663 @@
+// fluid3d_kernels.cuh -- device code of the 3D (and 2D poly6/spiky) SPH step.
+//
+// Two families of neighbour kernels:
+//   * "exact" kernels (thread per sorted particle) restate clCalculateDensity /
+//     clCalculateForces (libCL/phys/oclFluid3D.cl:150-255) operation for operation with
+//     round-to-nearest intrinsics (no FMA contraction, IEEE sqrt and division), visiting the
+//     27 (or 9) neighbour cells in the reference's z, y, x order. In REFERENCE_HASH mode that
+//     includes visiting a bucket twice when two neighbour cells hash to it. They reproduce the
+//     FP32 restatement bit for bit and serve the parity modes.
+//   * "brick" kernels (LINEAR_GRID only) are the fast path. A persistent CTA takes a brick of
+//     W cells along x, loads the cell table of the 9 (or 3) neighbour rows, copies those rows'
+//     contiguous particle ranges into shared memory with cp.async.bulk on one mbarrier, and
+//     each warp evaluates one target cell: lanes = (target, candidate stride) so candidate
+//     loads are shared-memory broadcasts; partial sums are combined with shuffles. FMA and
+//     rsqrt are used, so results agree with the restatement within FP32 tolerance.
+#pragma once
+
+#include "device.cuh"
+#include "internal.h"
+
+namespace gbsph {
+
+constexpr uint32_t EMPTY = 0xFFFFFFFFu;
+constexpr uint32_t REF_BUCKETS = 262144u;  // BUCKETS, libCL/phys/oclFluid3D.cl:32
+constexpr int BRICK_THREADS = 256;
+constexpr int BRICK_WARPS = BRICK_THREADS / 32;
+constexpr int BRICK_W_MAX = 16;
+constexpr int BRICK_SLOTS = BRICK_W_MAX + 2;
+
+// Kernel-side parameters, passed by value.
+struct KParams {
+    float dt, radius, h, mass, p0, rho0, stiff, cvisc, cpress, kconst, vlimit;
+    float h2;         // h*h
+    float r2_thresh;  // smallest float x with sqrtf(x) >= h, so (sqrtf(r2) < h) == (r2 < r2_thresh)
+    float4 gravity, box_min, box_max, origin;
+    int nx, ny, nz;
+    int key_mode, dims;
+    int end_bit;  // sort bits [0, end_bit)
+    int bw, bxn;  // brick width (cells) and bricks per x row
+    uint32_t n;
+    uint32_t table_cells;
+};
+
+// ---- keys ---------------------------------------------------------------------------------
+
+// gridPosition (libCL/phys/oclFluid3D.cl:34-42); LINEAR_GRID subtracts the grid origin.
+__device__ __forceinline__ void grid_position(const KParams& kp, float4 p, int& gx, int& gy, int& gz) {
+    if (kp.key_mode == GBSPH_KEY_LINEAR_GRID) {
+        p.x = __fsub_rn(p.x, kp.origin.x);
+        p.y = __fsub_rn(p.y, kp.origin.y);
+        p.z = __fsub_rn(p.z, kp.origin.z);
+    }
+    gx = (int)floorf(__fdiv_rn(p.x, kp.h));
+    gy = (int)floorf(__fdiv_rn(p.y, kp.h));
+    gz = kp.dims == 2 ? 0 : (int)floorf(__fdiv_rn(p.z, kp.h));
+}
+
+// hashKey (libCL/phys/oclFluid3D.cl:44-52).
+__device__ __forceinline__ uint32_t hash_key(int x, int y, int z) {
+    uint32_t n = (73856093u * (uint32_t)x) ^ (19349663u * (uint32_t)y) ^ (83492791u * (uint32_t)z);
+    return n % REF_BUCKETS;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+
+__device__ __forceinline__ uint32_t linear_key(const KParams& kp, int x, int y, int z) {
+    x = clampi(x, 0, kp.nx - 1);
+    y = clampi(y, 0, kp.ny - 1);
+    z = clampi(z, 0, kp.nz - 1);
+    return (uint32_t)x + (uint32_t)kp.nx * ((uint32_t)y + (uint32_t)kp.ny * (uint32_t)z);
+}
+
+__device__ __forceinline__ uint32_t particle_key(const KParams& kp, float4 p) {
+    int gx, gy, gz;
+    grid_position(kp, p, gx, gy, gz);
+    return kp.key_mode == GBSPH_KEY_LINEAR_GRID ? linear_key(kp, gx, gy, gz) : hash_key(gx, gy, gz);
+}
+
+// clHash (libCL/phys/oclFluid3D.cl:57-64) fused with the digit histogram of every sort pass
+// (the index is implicit: the first sort pass generates values 0..n-1). With CLEAR, the
+// linear cell table entries of the previous step's occupied cells are reset (the previous
+// sorted keys are still in `prev_keys`), replacing a full fill of the table.
+template <bool CLEAR>
+__global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos, KParams kp,
+                                              uint32_t* __restrict__ keys,
+                                              uint32_t* __restrict__ hist,
+                                              const uint32_t* __restrict__ prev_keys,
+                                              uint2* __restrict__ table) {
+    __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
+    for (int i = threadIdx.x; i < SORT_MAX_PASSES * SORT_RADIX; i += blockDim.x) s_h[i] = 0;
+    __syncthreads();
+    const int passes = sort_passes(0, kp.end_bit);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kp.n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = particle_key(kp, pos[i]);
+        keys[i] = k;
+        for (int p = 0; p < passes; ++p) {
+            const int shift = p * SORT_RADIX_BITS;
+            const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
+            atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
+        }
+        if (CLEAR) {
+            const uint32_t pk = prev_keys[i];
+            if ((i == 0 || prev_keys[i - 1] != pk) && pk < kp.table_cells) table[pk] = make_uint2(EMPTY, EMPTY);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * SORT_RADIX; i += blockDim.x)
+        if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
+}
+
+// clReorder (libCL/phys/oclFluid3D.cl:66-72), used when the gather is not fused into the
+// last sort pass.
+__global__ void k_reorder(const uint32_t* __restrict__ index, const float4* __restrict__ pos,
+                          const float4* __restrict__ vel, float4* __restrict__ spos,
+                          float4* __restrict__ svel, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = index[i];
+    spos[i] = pos[s];
+    svel[i] = vel[s];
+}
+
+// Cell bounds into the interleaved LINEAR_GRID table, plus the list of occupied bricks
+// (brick id = x/W + bxn*(y + ny*z)), appended through an atomic counter.
+__global__ void k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
+                                uint2* __restrict__ table, uint32_t* __restrict__ bricks,
+                                uint32_t* __restrict__ n_bricks, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    const uint32_t k = keys[i];
+    if (k >= kp.table_cells) {
+        atomicOr(err, DEV_ERR_KEY_RANGE);
+        return;
+    }
+    const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
+    const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
+    if (k != prev) table[k].x = i;
+    if (k != next) table[k].y = i + 1;
+    const uint32_t nx = (uint32_t)kp.nx, bw = (uint32_t)kp.bw;
+    const uint32_t bid = (k % nx) / bw + (uint32_t)kp.bxn * (k / nx);
+    const uint32_t pbid = (prev == EMPTY) ? EMPTY : (prev % nx) / bw + (uint32_t)kp.bxn * (prev / nx);
+    if (bid != pbid) bricks[atomicAdd(n_bricks, 1u)] = bid;
+}
+
+// Splits the interleaved table into two arrays (for inspection through the ABI).
+__global__ void k_table_split(const uint2* __restrict__ table, uint32_t cells,
+                              uint32_t* __restrict__ cs, uint32_t* __restrict__ ce) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cells) return;
+    const uint2 e = table[i];
+    cs[i] = e.x;
+    ce[i] = e.x == EMPTY ? EMPTY : e.y;
+}
+
+// ---- exact (reference-order) neighbour kernels ---------------------------------------------
+
+struct SplitTable {  // REFERENCE_HASH: bfCellStart / bfCellEnd
+    const uint32_t* cs;
+    const uint32_t* ce;
+    __device__ __forceinline__ uint2 get(uint32_t k) const { return make_uint2(cs[k], ce[k]); }
+};
+struct PairTable {  // LINEAR_GRID: interleaved
+    const uint2* t;
+    __device__ __forceinline__ uint2 get(uint32_t k) const { return t[k]; }
+};
+
+// Calls f(start, end) for each non-empty neighbour cell in the reference's visiting order.
+template <int MODE, class Table, class F>
+__device__ __forceinline__ void for_each_neighbour_cell(const KParams& kp, const Table& tab, float4 p, F&& f) {
+    int gx, gy, gz;
+    grid_position(kp, p, gx, gy, gz);
+    const int zr = kp.dims == 2 ? 0 : 1;
+    if (MODE == GBSPH_KEY_LINEAR_GRID) {
+        gx = clampi(gx, 0, kp.nx - 1);
+        gy = clampi(gy, 0, kp.ny - 1);
+        gz = kp.dims == 2 ? 0 : clampi(gz, 0, kp.nz - 1);
+    }
+    for (int z = -zr; z <= zr; z++)
+        for (int y = -1; y <= 1; y++)
+            for (int x = -1; x <= 1; x++) {
+                uint32_t cell;
+                if (MODE == GBSPH_KEY_LINEAR_GRID) {
+                    const int cx = gx + x, cy = gy + y, cz = gz + z;
+                    if (cx < 0 || cy < 0 || cz < 0 || cx >= kp.nx || cy >= kp.ny || cz >= kp.nz) continue;
+                    cell = (uint32_t)cx + (uint32_t)kp.nx * ((uint32_t)cy + (uint32_t)kp.ny * (uint32_t)cz);
+                } else {
+                    cell = hash_key(gx + x, gy + y, gz + z);
+                }
+                const uint2 e = tab.get(cell);
+                if (e.x == EMPTY) continue;
+                f(e.x, e.y);
+            }
+}
+
+// fast_length of (a - b) with w = 0, evaluated as ((x*x + y*y) + z*z), correctly rounded sqrt.
+__device__ __forceinline__ float exact_len(float vx, float vy, float vz) {
+    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz)));
+}
+
+// clCalculateDensity, libCL/phys/oclFluid3D.cl:150-200.
+template <int MODE, class Table>
+__global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos, float4* __restrict__ svel,
+                                                       Table tab, KParams kp) {
+    const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
+    if (particle >= kp.n) return;
+    const float4 posI = spos[particle];
+    float density = 0.0f;
+    int count = 0;
+    for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
+        for (uint32_t j = start; j < end; j++) {
+            if (j == particle) continue;
+            const float4 pj = spos[j];
+            const float vlen = exact_len(__fsub_rn(posI.x, pj.x), __fsub_rn(posI.y, pj.y), __fsub_rn(posI.z, pj.z));
+            if (vlen < kp.h) {
+                const float t = __fsub_rn(__fmul_rn(kp.h, kp.h), __fmul_rn(vlen, vlen));
+                density = __fadd_rn(density, __fmul_rn(__fmul_rn(t, t), t));
+                count++;
+            }
+        }
+    });
+    // The reference writes .w in place while other work-items read .xyz only; here every
+    // thread has read all it needs before any write lands on a different particle, because
+    // the writes only touch .w which no thread of this kernel reads.
+    if (count > 2) {
+        density = fmaxf(1.0f, __fmul_rn(__fmul_rn(kp.mass, kp.kconst), density));
+        reinterpret_cast<float*>(spos)[4 * (size_t)particle + 3] = density;
+        reinterpret_cast<float*>(svel)[4 * (size_t)particle + 3] =
+            __fadd_rn(kp.p0, __fmul_rn(kp.stiff, __fsub_rn(density, kp.rho0)));
+    } else {
+        reinterpret_cast<float*>(spos)[4 * (size_t)particle + 3] = kp.rho0;
+        reinterpret_cast<float*>(svel)[4 * (size_t)particle + 3] = kp.p0;
+    }
+}
+
+// clCalculateForces, libCL/phys/oclFluid3D.cl:202-255: force[index[i]] += SPH force, w = 0.
+template <int MODE, class Table>
+__global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__ spos,
+                                                      const float4* __restrict__ svel,
+                                                      float4* __restrict__ force,
+                                                      const uint32_t* __restrict__ index,
+                                                      Table tab, KParams kp) {
+    const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
+    if (particle >= kp.n) return;
+    const float4 posI = spos[particle], velI = svel[particle];
+    float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+    for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
+        for (uint32_t j = start; j < end; j++) {
+            if (j == particle) continue;
+            const float4 posJ = spos[j];
+            const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
+            const float vlen = exact_len(vx, vy, vz);
+            if (vlen < kp.h) {
+                const float4 velJ = svel[j];
+                const float density2 = __fmul_rn(posI.w, posJ.w);
+                const float s = __fdiv_rn(__fadd_rn(velI.w, velJ.w), density2);
+                const float hr = __fsub_rn(kp.h, vlen);
+                px = __fadd_rn(px, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vx, vlen), hr), hr)));
+                py = __fadd_rn(py, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vy, vlen), hr), hr)));
+                pz = __fadd_rn(pz, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vz, vlen), hr), hr)));
+                qx = __fadd_rn(qx, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.x, velI.x), density2), hr));
+                qy = __fadd_rn(qy, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.y, velI.y), density2), hr));
+                qz = __fadd_rn(qz, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.z, velI.z), density2), hr));
+            }
+        }
+    });
+    const uint32_t o = index[particle];
+    float4 f = force[o];
+    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, px), __fmul_rn(kp.cvisc, qx)), kp.mass));
+    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, py), __fmul_rn(kp.cvisc, qy)), kp.mass));
+    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, pz), __fmul_rn(kp.cvisc, qz)), kp.mass));
+    f.w = 0.0f;
+    force[o] = f;
+}
+
+// ---- post stages ---------------------------------------------------------------------------
+
+// repulsionForce walls of clClipBox (libCL/phys/oclFluid3D.cl:304-361): EPSILON 1e-5,
+// stiffness 2000, damping 256, in the order y-min, y-max, z-min, z-max, x-min, x-max.
+__device__ __forceinline__ void add_wall(float& fa, float& fw, float sign, float diff, float vn) {
+    if (diff > 0.00001f) {
+        const float mag = __fsub_rn(__fmul_rn(2000.0f, diff), __fmul_rn(256.0f, __fmul_rn(sign, vn)));
+        fa = __fadd_rn(fa, __fmul_rn(sign, mag));
+        fw = __fadd_rn(fw, __fmul_rn(0.0f, mag));
+    }
+}
+
+__device__ __forceinline__ float4 clip_box_force(const KParams& kp, float4 pos, float4 vel, float4 f) {
+    const float r = kp.radius;
+    add_wall(f.y, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.y, kp.box_min.y)), vel.y);
+    add_wall(f.y, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.y, pos.y)), vel.y);
+    if (kp.dims != 2) {
+        add_wall(f.z, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.z, kp.box_min.z)), vel.z);
+        add_wall(f.z, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.z, pos.z)), vel.z);
+    }
+    add_wall(f.x, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.x, kp.box_min.x)), vel.x);
+    add_wall(f.x, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.x, pos.x)), vel.x);
+    return f;
+}
+
+// clIntegrateForce (libCL/phys/oclFluid3D.cl:258-271): clamp |F|, v += F*dt on 4 lanes.
+__device__ __forceinline__ float4 integrate_force(const KParams& kp, float4 v, float4 f) {
+    const float speed = __fsqrt_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(f.x, f.x), __fmul_rn(f.y, f.y)),
+                                                       __fmul_rn(f.z, f.z)), __fmul_rn(f.w, f.w)));
+    if (speed > kp.vlimit) {
+        const float s = __fdiv_rn(kp.vlimit, speed);
+        f.x = __fmul_rn(f.x, s);
+        f.y = __fmul_rn(f.y, s);
+        f.z = __fmul_rn(f.z, s);
+        f.w = __fmul_rn(f.w, s);
+    }
+    v.x = __fadd_rn(v.x, __fmul_rn(f.x, kp.dt));
+    v.y = __fadd_rn(v.y, __fmul_rn(f.y, kp.dt));
+    v.z = __fadd_rn(v.z, __fmul_rn(f.z, kp.dt));
+    v.w = __fadd_rn(v.w, __fmul_rn(f.w, kp.dt));
+    return v;
+}
+
+// clIntegrateVelocity (libCL/phys/oclFluid3D.cl:284-291): all four lanes.
+__device__ __forceinline__ float4 integrate_velocity(const KParams& kp, float4 p, float4 v) {
+    return make_float4(__fadd_rn(p.x, __fmul_rn(v.x, kp.dt)), __fadd_rn(p.y, __fmul_rn(v.y, kp.dt)),
+                       __fadd_rn(p.z, __fmul_rn(v.z, kp.dt)), __fadd_rn(p.w, __fmul_rn(v.w, kp.dt)));
+}
+
+__global__ void k_clip_box(const float4* __restrict__ spos, const float4* __restrict__ svel,
+                           float4* __restrict__ force, const uint32_t* __restrict__ index, KParams kp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    const uint32_t o = index[i];
+    force[o] = clip_box_force(kp, spos[i], svel[i], force[o]);
+}
+
+__global__ void k_integrate_force(float4* __restrict__ vel, const float4* __restrict__ force, KParams kp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    vel[i] = integrate_force(kp, vel[i], force[i]);
+}
+
+__global__ void k_gravity(float4* __restrict__ force, KParams kp) {  // clGravity, :294-298
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    force[i] = kp.gravity;
+}
+
+__global__ void k_integrate_velocity(float4* __restrict__ pos, const float4* __restrict__ vel, KParams kp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    pos[i] = integrate_velocity(kp, pos[i], vel[i]);
+}
+
+// clip + integrate-force + gravity + integrate-velocity in one pass over sorted slots.
+// Equivalent to the four reference kernels because index is a permutation.
+__global__ void k_post_fused(const float4* __restrict__ spos, const float4* __restrict__ svel,
+                             const uint32_t* __restrict__ index, float4* __restrict__ pos,
+                             float4* __restrict__ vel, float4* __restrict__ force, KParams kp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    const uint32_t o = index[i];
+    const float4 f = clip_box_force(kp, spos[i], svel[i], force[o]);
+    const float4 v = integrate_force(kp, vel[o], f);
+    vel[o] = v;
+    force[o] = kp.gravity;
+    pos[o] = integrate_velocity(kp, pos[o], v);
+}
+
+// ---- brick (fast, LINEAR_GRID) neighbour kernels ---------------------------------------------
+
+struct BrickShared {
+    uint32_t cnt[9][BRICK_SLOTS];
+    uint32_t st[9][BRICK_SLOTS];
+    uint32_t off[9][BRICK_SLOTS + 1];  // lower bounds of each cell inside the row's range
+    uint32_t lo[9];                    // first sorted index of the row's range
+    uint32_t rcnt[9];
+    uint32_t base[9];                  // offset of the row in the staging buffer
+    uint32_t total;
+    uint32_t brick;
+    uint32_t abort;
+    unsigned long long bar;
+};
+
+// Loads the brick's geometry and neighbour-row ranges into S; thread 0 starts the bulk copies
+// of `n_arrays` float4 arrays (pos, optionally vel) when the rows fit in `cap`.
+// Returns the brick's first cell x and cell count through x0/ncell.
+template <int DIMS>
+__device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, uint32_t bid,
+                                            const uint2* __restrict__ table, int& x0, int& ncell) {
+    constexpr int R = DIMS == 3 ? 9 : 3;
+    const int W = kp.bw;
+    const int bx = (int)(bid % (uint32_t)kp.bxn);
+    const uint32_t yz = bid / (uint32_t)kp.bxn;
+    const int y = (int)(yz % (uint32_t)kp.ny);
+    const int z = (int)(yz / (uint32_t)kp.ny);
+    x0 = bx * W;
+    ncell = min(W, kp.nx - x0);
+    const int t = threadIdx.x;
+    for (int idx = t; idx < R * (W + 2); idx += BRICK_THREADS) {
+        const int r = idx / (W + 2), c = idx - r * (W + 2);
+        const int cy = y + (r % 3) - 1;
+        const int cz = DIMS == 3 ? z + (r / 3) - 1 : 0;
+        const int cx = x0 - 1 + c;
+        uint32_t cnt = 0, st = 0;
+        if (cx >= 0 && cx < kp.nx && cy >= 0 && cy < kp.ny && cz >= 0 && cz < kp.nz) {
+            const uint2 e = table[(uint32_t)cx + (uint32_t)kp.nx * ((uint32_t)cy + (uint32_t)kp.ny * (uint32_t)cz)];
+            if (e.x != EMPTY) {
+                cnt = e.y - e.x;
+                st = e.x;
+            }
+        }
+        S.cnt[r][c] = cnt;
+        S.st[r][c] = st;
+    }
+    __syncthreads();
+    if (t < R) {
+        uint32_t acc = 0, lo = EMPTY;
+        for (int c = 0; c < W + 2; ++c) {
+            S.off[t][c] = acc;
+            if (S.cnt[t][c]) {
+                if (lo == EMPTY) lo = S.st[t][c];
+                acc += S.cnt[t][c];
+            }
+        }
+        S.off[t][W + 2] = acc;
+        S.lo[t] = lo == EMPTY ? 0u : lo;
+        S.rcnt[t] = acc;
+    }
+    __syncthreads();
+}
+
+// Thread 0: compute row bases and issue the copies. Returns (to all threads, after a
+// barrier) whether the brick's rows are staged in shared memory.
+template <int DIMS, int NARR>
+__device__ __forceinline__ bool brick_stage(BrickShared& S, float4* s_buf, uint32_t cap,
+                                            const float4* __restrict__ a0, const float4* __restrict__ a1) {
+    constexpr int R = DIMS == 3 ? 9 : 3;
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int r = 0; r < R; ++r) {
+            S.base[r] = acc;
+            acc += S.rcnt[r];
+        }
+        S.total = acc;
+        if (acc <= cap && acc > 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 16u * NARR);
+            for (int r = 0; r < R; ++r) {
+                if (!S.rcnt[r]) continue;
+                bulk_g2s(s_buf + S.base[r], a0 + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                if (NARR > 1)
+                    bulk_g2s(s_buf + cap + S.base[r], a1 + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+            }
+        }
+    }
+    __syncthreads();
+    return S.total <= cap && S.total > 0;
+}
+
+// Waits for the staged copies. On timeout every thread learns it through S.abort.
+__device__ __forceinline__ bool brick_wait(BrickShared& S, uint32_t& phase, uint32_t* err) {
+    bool ok = mbar_wait_bounded(reinterpret_cast<uint64_t*>(&S.bar), phase);
+    if (!ok) atomicOr(err, DEV_ERR_MBAR_TIMEOUT);
+    ok = __syncthreads_and(ok);
+    phase ^= 1u;
+    if (!ok && threadIdx.x == 0) {
+        // drain the copies still in flight (bounded) before this CTA's shared memory goes away
+        mbar_wait_bounded(reinterpret_cast<uint64_t*>(&S.bar), phase ^ 1u);
+    }
+    return ok;
+}
+
+// Tree reduction over the Q lanes {q*tg + ti} that share a target.
+__device__ __forceinline__ float reduce_q(float v, uint32_t q, uint32_t Q, uint32_t tg) {
+    for (uint32_t s = 1; s < Q; s <<= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, v, s * tg);
+        if ((q & (2 * s - 1)) == 0 && q + s < Q) v += o;
+    }
+    return v;
+}
+
+// Density + pressure for every particle of the occupied bricks (persistent CTAs).
+// Writes sorted position .w = density and sorted velocity .w = pressure, as
+// clCalculateDensity does (libCL/phys/oclFluid3D.cl:189-199).
+template <int DIMS>
+__global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
+                                                                 float4* __restrict__ svel,
+                                                                 const uint2* __restrict__ table,
+                                                                 const uint32_t* __restrict__ bricks,
+                                                                 uint32_t* counters, KParams kp,
+                                                                 uint32_t cap, uint32_t* err) {
+    constexpr int R = DIMS == 3 ? 9 : 3;
+    constexpr int RC = DIMS == 3 ? 4 : 1;  // the brick's own row
+    extern __shared__ float4 s_buf[];
+    __shared__ BrickShared S;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const uint32_t n_bricks = counters[0];
+    for (;;) {
+        if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
+        __syncthreads();
+        const uint32_t b = S.brick;
+        if (b >= n_bricks) break;
+        int x0, ncell;
+        brick_setup<DIMS>(S, kp, bricks[b], table, x0, ncell);
+        const bool staged = brick_stage<DIMS, 1>(S, s_buf, cap, spos, nullptr);
+        if (staged && !brick_wait(S, phase, err)) return;
+        for (int c = warp; c < ncell; c += BRICK_WARPS) {
+            const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
+            for (uint32_t g0 = 0; g0 < nt; g0 += 32) {
+                const uint32_t tg = min(32u, nt - g0), Q = 32u / tg;
+                const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
+                const bool active = q < Q;
+                const uint32_t tl = t0 + g0 + ti;
+                const uint32_t gi = S.lo[RC] + tl;
+                const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
+                float acc = 0.0f, cntf = 0.0f;
+                if (active) {
+#pragma unroll 1
+                    for (int r = 0; r < R; ++r) {
+                        const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
+                        const uint32_t rlo = S.lo[r], hi = S.off[r][c + 3];
+#pragma unroll 4
+                        for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
+                            const float4 pj = rp[j];
+                            const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                            float r2 = fmaf(dy, dy, dx * dx);
+                            if (DIMS == 3) {
+                                const float dz = pi.z - pj.z;
+                                r2 = fmaf(dz, dz, r2);
+                            }
+                            if (r2 < kp.r2_thresh && rlo + j != gi) {
+                                const float tt = kp.h2 - r2;
+                                acc = fmaf(tt * tt, tt, acc);
+                                cntf += 1.0f;
+                            }
+                        }
+                    }
+                }
+                acc = reduce_q(acc, q, Q, tg);
+                cntf = reduce_q(cntf, q, Q, tg);
+                if (active && q == 0) {
+                    float rho = kp.rho0, p = kp.p0;
+                    if (cntf > 2.5f) {
+                        rho = fmaxf(1.0f, kp.mass * kp.kconst * acc);
+                        p = kp.p0 + kp.stiff * (rho - kp.rho0);
+                    }
+                    spos[gi] = make_float4(pi.x, pi.y, pi.z, rho);
+                    reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
+                }
+            }
+        }
+    }
+}
+
+// Forces (pressure + viscosity) for every particle of the occupied bricks. With FUSED the
+// clip-box, integrate-force, gravity and integrate-velocity stages follow in registers;
+// otherwise the SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
+template <int DIMS, bool FUSED>
+__global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __restrict__ spos,
+                                                               const float4* __restrict__ svel,
+                                                               const uint32_t* __restrict__ index,
+                                                               float4* __restrict__ pos,
+                                                               float4* __restrict__ vel,
+                                                               float4* __restrict__ force,
+                                                               const uint2* __restrict__ table,
+                                                               const uint32_t* __restrict__ bricks,
+                                                               uint32_t* counters, KParams kp,
+                                                               uint32_t cap, uint32_t* err) {
+    constexpr int R = DIMS == 3 ? 9 : 3;
+    constexpr int RC = DIMS == 3 ? 4 : 1;
+    extern __shared__ float4 s_buf[];  // [cap] positions, then [cap] velocities
+    __shared__ BrickShared S;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (t == 0) {
+        mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const uint32_t n_bricks = counters[0];
+    for (;;) {
+        if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
+        __syncthreads();
+        const uint32_t b = S.brick;
+        if (b >= n_bricks) break;
+        int x0, ncell;
+        brick_setup<DIMS>(S, kp, bricks[b], table, x0, ncell);
+        const bool staged = brick_stage<DIMS, 2>(S, s_buf, cap, spos, svel);
+        if (staged && !brick_wait(S, phase, err)) return;
+        for (int c = warp; c < ncell; c += BRICK_WARPS) {
+            const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
+            for (uint32_t g0 = 0; g0 < nt; g0 += 32) {
+                const uint32_t tg = min(32u, nt - g0), Q = 32u / tg;
+                const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
+                const bool active = q < Q;
+                const uint32_t tl = t0 + g0 + ti;
+                const uint32_t gi = S.lo[RC] + tl;
+                const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
+                const float4 vi = staged ? s_buf[cap + S.base[RC] + tl] : svel[gi];
+                const float inv_rho_i = 1.0f / pi.w;
+                float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
+                if (active) {
+#pragma unroll 1
+                    for (int r = 0; r < R; ++r) {
+                        const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
+                        const float4* rv = staged ? s_buf + cap + S.base[r] : svel + S.lo[r];
+                        const uint32_t rlo = S.lo[r], hi = S.off[r][c + 3];
+#pragma unroll 2
+                        for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
+                            const float4 pj = rp[j];
+                            const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                            const float dz = DIMS == 3 ? pi.z - pj.z : 0.0f;
+                            float r2 = fmaf(dy, dy, dx * dx);
+                            if (DIMS == 3) r2 = fmaf(dz, dz, r2);
+                            if (r2 < kp.r2_thresh && rlo + j != gi) {
+                                const float4 vj = rv[j];
+                                const float inv = rsqrtf(r2);
+                                const float vlen = r2 * inv;
+                                const float hr = kp.h - vlen;
+                                const float dd = inv_rho_i / pj.w;           // 1/(rho_i rho_j)
+                                const float sp = (vi.w + vj.w) * dd * hr * hr * inv;
+                                px = fmaf(sp, dx, px);
+                                py = fmaf(sp, dy, py);
+                                pz = fmaf(sp, dz, pz);
+                                const float cvv = hr * dd;
+                                qx = fmaf(vj.x - vi.x, cvv, qx);
+                                qy = fmaf(vj.y - vi.y, cvv, qy);
+                                qz = fmaf(vj.z - vi.z, cvv, qz);
+                            }
+                        }
+                    }
+                }
+                px = reduce_q(px, q, Q, tg);
+                py = reduce_q(py, q, Q, tg);
+                pz = reduce_q(pz, q, Q, tg);
+                qx = reduce_q(qx, q, Q, tg);
+                qy = reduce_q(qy, q, Q, tg);
+                qz = reduce_q(qz, q, Q, tg);
+                if (active && q == 0) {
+                    const uint32_t o = index[gi];
+                    float4 f = force[o];
+                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, px), __fmul_rn(kp.cvisc, qx)), kp.mass));
+                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, py), __fmul_rn(kp.cvisc, qy)), kp.mass));
+                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, pz), __fmul_rn(kp.cvisc, qz)), kp.mass));
+                    f.w = 0.0f;
+                    if (FUSED) {
+                        f = clip_box_force(kp, pi, vi, f);
+                        const float4 v = integrate_force(kp, vel[o], f);
+                        vel[o] = v;
+                        force[o] = kp.gravity;
+                        pos[o] = integrate_velocity(kp, pos[o], v);
+                    } else {
+                        force[o] = f;
+                    }
+                }
+            }
+        }
+    }
+}
+
+}  // namespace gbsph

@@ -1,0 +1,453 @@
+// radix_sort.cu -- stable LSD radix sort of (uint32 key, uint32 value) pairs for sm_103a.
+//
+// Replaces libCL's oclRadixSort (libCL/sort/oclRadixSort.cpp:62-144,
+// libCL/sort/oclRadixSort.cl:20-222): same contract (stable sort on key bits
+// [start_bit, end_bit), in place, counts must match, bit range a multiple of 4), different
+// algorithm. The reference runs 4-bit passes of four kernels each, with single-thread serial
+// prefix sums. Here every 8-bit digit is one "one-sweep" pass:
+//   * one histogram kernel counts the digits of every pass in a single read of the keys;
+//   * each pass kernel takes a tile of 4096 keys (tile id from an atomic counter, so tiles
+//     are started in order and the look-back always waits on running CTAs), ranks keys
+//     inside each warp with warp ballots (peers of the same digit = AND of 8 ballots),
+//     combines the warps' counts, publishes the tile's per-digit count, and finds the
+//     exclusive prefix over earlier tiles by decoupled look-back on 32-bit status words
+//     (2 flag bits + 30 count bits). The look-back spin is bounded: on timeout the kernel
+//     sets an error bit, publishes anyway (so later tiles never hang) and finishes.
+//   * keys are scattered through shared memory so each digit's run is written contiguously.
+// The last pass can gather float4 payloads by the sorted value (the fluid's reorder stage).
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "device.cuh"
+#include "internal.h"
+
+namespace gbsph {
+namespace {
+
+constexpr uint32_t FLAG_AGG = 1u << 30;
+constexpr uint32_t FLAG_PREFIX = 2u << 30;
+constexpr uint32_t COUNT_MASK = (1u << 30) - 1u;
+constexpr int SORT_WARPS = SORT_THREADS / 32;
+
+static_assert(SORT_THREADS == SORT_RADIX, "one thread per digit in the per-digit phases");
+
+// Exclusive scan of one value per thread over a 256-thread block. `s_tmp` holds 8 words.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_tmp) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < SORT_WARPS ? s_tmp[lane] : 0u;
+        uint32_t incl = w;
+#pragma unroll
+        for (int o = 1; o < SORT_WARPS; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane < SORT_WARPS) s_tmp[lane] = incl - w;
+    }
+    __syncthreads();
+    uint32_t r = x - v + s_tmp[warp];
+    __syncthreads();  // s_tmp may be reused by the caller
+    return r;
+}
+
+__global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
+                                                   int start_bit, int end_bit,
+                                                   uint32_t* __restrict__ hist) {
+    __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
+    for (int i = threadIdx.x; i < SORT_MAX_PASSES * SORT_RADIX; i += blockDim.x) s_h[i] = 0;
+    __syncthreads();
+    const int passes = sort_passes(start_bit, end_bit);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = __ldg(keys + i);
+        for (int p = 0; p < passes; ++p) {
+            const int shift = start_bit + p * SORT_RADIX_BITS;
+            const int bits = min(SORT_RADIX_BITS, end_bit - shift);
+            atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * SORT_RADIX; i += blockDim.x)
+        if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
+}
+
+template <bool IOTA, int NGATHER>
+__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
+    const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
+    int bits, int pass, uint32_t tiles, uint32_t* __restrict__ scratch, uint32_t* err,
+    SortGather gather) {
+    __shared__ uint32_t s_keys[SORT_TILE];
+    __shared__ uint32_t s_vals[SORT_TILE];
+    __shared__ uint32_t s_whist[SORT_WARPS * SORT_RADIX];
+    __shared__ uint32_t s_tile_start[SORT_RADIX];
+    __shared__ uint32_t s_base[SORT_RADIX];
+    __shared__ uint32_t s_tmp[SORT_WARPS];
+    __shared__ uint32_t s_tile;
+
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t* hist = scratch + pass * SORT_RADIX;
+    uint32_t* counter = scratch + 4096 / 4 + pass;
+    uint32_t* status = scratch + SORT_HEADER_BYTES / 4 + (size_t)pass * tiles * SORT_RADIX;
+
+    if (t == 0) s_tile = atomicAdd(counter, 1u);
+    for (int i = t; i < SORT_WARPS * SORT_RADIX; i += SORT_THREADS) s_whist[i] = 0;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * SORT_TILE;
+    const uint32_t mask = (1u << bits) - 1u;
+
+    // Load: warp-striped, so item order inside the tile is (warp, i, lane) == index order.
+    uint32_t k[SORT_ITEMS], v[SORT_ITEMS], r[SORT_ITEMS];
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t idx = base + (uint32_t)(warp * 32 * SORT_ITEMS + i * 32 + lane);
+        const bool in = idx < n;
+        k[i] = in ? keys_in[idx] : 0xFFFFFFFFu;  // padding sorts last in the top digit
+        v[i] = IOTA ? idx : (in ? vals_in[idx] : 0u);
+    }
+
+    // Rank within the warp: peers of equal digit via ballots; the lowest peer lane updates
+    // the warp's private digit counter and broadcasts the old value.
+    uint32_t* wh = s_whist + warp * SORT_RADIX;
+    const uint32_t lt = lanemask_lt();
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t d = (k[i] >> shift) & mask;
+        uint32_t peers = 0xffffffffu;
+        for (int b = 0; b < bits; ++b) {
+            const uint32_t bit = (d >> b) & 1u;
+            const uint32_t m = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? m : ~m;
+        }
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if ((uint32_t)lane == leader) {
+            old = wh[d];
+            wh[d] = old + __popc(peers);
+        }
+        old = __shfl_sync(0xffffffffu, old, leader);
+        r[i] = old + __popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // Thread t owns digit t: warp-exclusive offsets, tile count, tile-local start.
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < SORT_WARPS; ++w) {
+        const uint32_t c = s_whist[w * SORT_RADIX + t];
+        s_whist[w * SORT_RADIX + t] = cnt;
+        cnt += c;
+    }
+    const uint32_t tstart = block_exclusive_scan(cnt, s_tmp);
+    s_tile_start[t] = tstart;
+    const uint32_t goff = block_exclusive_scan(hist[t], s_tmp);
+
+    // Decoupled look-back for digit t.
+    uint32_t excl = 0;
+    if (tile == 0) {
+        st_relaxed_gpu(&status[t], FLAG_PREFIX | cnt);
+    } else {
+        st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_AGG | cnt);
+        int pred = (int)tile - 1;
+        uint32_t spins = 0;
+        while (pred >= 0) {
+            const uint32_t s = ld_relaxed_gpu(&status[(size_t)pred * SORT_RADIX + t]);
+            if ((s & ~COUNT_MASK) == 0u) {
+                if (++spins > SPIN_LIMIT) {
+                    atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
+                    break;
+                }
+                if (spins > 32) __nanosleep(64);
+                continue;
+            }
+            excl += s & COUNT_MASK;
+            if (s & FLAG_PREFIX) break;
+            --pred;
+        }
+        st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_PREFIX | ((excl + cnt) & COUNT_MASK));
+    }
+    s_base[t] = goff + excl - tstart;
+    __syncthreads();
+
+    // Tile-local sorted order in shared memory.
+#pragma unroll
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t d = (k[i] >> shift) & mask;
+        const uint32_t pos = s_tile_start[d] + s_whist[warp * SORT_RADIX + d] + r[i];
+        s_keys[pos] = k[i];
+        s_vals[pos] = v[i];
+    }
+    __syncthreads();
+
+    // Each digit's run goes to one contiguous range of the output.
+    const uint32_t valid = min((uint32_t)SORT_TILE, n - base);
+#pragma unroll 4
+    for (int i = 0; i < SORT_ITEMS; ++i) {
+        const uint32_t j = (uint32_t)(i * SORT_THREADS + t);
+        if (j < valid) {
+            const uint32_t key = s_keys[j], val = s_vals[j];
+            const uint32_t dst = s_base[(key >> shift) & mask] + j;
+            keys_out[dst] = key;
+            vals_out[dst] = val;
+            if (NGATHER > 0) gather.dst[0][dst] = __ldg(gather.src[0] + val);
+            if (NGATHER > 1) gather.dst[1][dst] = __ldg(gather.src[1] + val);
+        }
+    }
+}
+
+__global__ void k_cell_bounds(const uint32_t* __restrict__ keys, uint32_t n,
+                              uint32_t* __restrict__ cs, uint32_t* __restrict__ ce,
+                              uint32_t n_cells, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = keys[i];
+    if (k >= n_cells) {
+        atomicOr(err, DEV_ERR_KEY_RANGE);
+        return;
+    }
+    if (i == 0) {
+        cs[k] = 0;
+    } else {
+        const uint32_t prev = keys[i - 1];
+        if (prev != k) {
+            cs[k] = i;
+            if (prev < n_cells) ce[prev] = i;
+        }
+    }
+    if (i == n - 1) ce[k] = n;
+}
+
+template <bool IOTA>
+cudaError_t launch_pass(int ngather, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                        uint32_t* vout, uint32_t n, int shift, int bits, int pass, uint32_t tiles,
+                        uint32_t* scratch, uint32_t* err, const SortGather& g, cudaStream_t s) {
+    if (ngather == 2)
+        k_onesweep<IOTA, 2><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    else if (ngather == 1)
+        k_onesweep<IOTA, 1><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    else
+        k_onesweep<IOTA, 0><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t onesweep_scratch_bytes(uint32_t n, int passes) {
+    return SORT_HEADER_BYTES + (size_t)std::max(passes, 1) * sort_tiles(std::max(n, 1u)) * SORT_RADIX * 4;
+}
+
+cudaError_t onesweep_prepare(void* scratch, uint32_t n, int passes, cudaStream_t s) {
+    return cudaMemsetAsync(scratch, 0, onesweep_scratch_bytes(n, passes), s);
+}
+
+cudaError_t onesweep_histogram(const uint32_t* keys, uint32_t n, int start_bit, int end_bit,
+                               void* scratch, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const int threads = 512;
+    int blocks = (int)std::min<uint64_t>(((uint64_t)n + threads * 8 - 1) / (threads * 8), (uint64_t)num_sms() * 4);
+    blocks = std::max(blocks, 1);
+    k_sort_hist<<<blocks, threads, 0, s>>>(keys, n, start_bit, end_bit, (uint32_t*)scratch);
+    return cudaGetLastError();
+}
+
+cudaError_t onesweep_passes(const OnesweepArgs& a, cudaStream_t s) {
+    const int P = sort_passes(a.start_bit, a.end_bit);
+    if (a.n == 0 || P == 0) return cudaSuccess;
+    const uint32_t tiles = sort_tiles(a.n);
+    const uint32_t* kin = a.keys_in;
+    const uint32_t* vin = a.vals_in;
+    for (int p = 0; p < P; ++p) {
+        const bool last = p == P - 1;
+        uint32_t* kout = last ? a.keys_out : a.tmp_keys[p & 1];
+        uint32_t* vout = last ? a.vals_out : a.tmp_vals[p & 1];
+        const int shift = a.start_bit + p * SORT_RADIX_BITS;
+        const int bits = std::min(SORT_RADIX_BITS, a.end_bit - shift);
+        const int ng = last ? a.gather.n_gather : 0;
+        cudaError_t e = (vin == nullptr)
+            ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, tiles, (uint32_t*)a.scratch, a.err, a.gather, s)
+            : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, tiles, (uint32_t*)a.scratch, a.err, a.gather, s);
+        if (e != cudaSuccess) return e;
+        kin = kout;
+        vin = vout;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t cell_bounds_launch(const uint32_t* sorted_keys, uint32_t n, uint32_t* cell_start,
+                               uint32_t* cell_end, uint32_t n_cells, uint32_t* err,
+                               cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(cell_start, 0xFF, (size_t)n_cells * 4, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(cell_end, 0xFF, (size_t)n_cells * 4, s);
+    if (e != cudaSuccess || n == 0) return e;
+    k_cell_bounds<<<(n + 255) / 256, 256, 0, s>>>(sorted_keys, n, cell_start, cell_end, n_cells, err);
+    return cudaGetLastError();
+}
+
+}  // namespace gbsph
+
+// ------------------------------------------------------------------------------------------
+// C ABI: the oclRadixSort replacement.
+// ------------------------------------------------------------------------------------------
+struct gbsph_radix_sort_s {
+    int device = 0;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint32_t* tmp = nullptr;  // 4 arrays of tmp_cap: keys0, vals0, keys1, vals1
+    size_t tmp_cap = 0;
+    uint32_t* err = nullptr;
+    std::string last_error;
+};
+
+using namespace gbsph;
+
+namespace {
+
+int fit_scratch(gbsph_radix_sort_s* h, size_t bytes) {
+    if (h->scratch_bytes >= bytes) return GBSPH_OK;
+    if (h->scratch) cudaFree(h->scratch);
+    h->scratch = nullptr;
+    h->scratch_bytes = 0;
+    if (cudaMalloc(&h->scratch, bytes) != cudaSuccess)
+        return fail(&h->last_error, GBSPH_ERR_OUT_OF_MEMORY, "radix sort: scratch allocation failed");
+    h->scratch_bytes = bytes;
+    return GBSPH_OK;
+}
+
+int fit_tmp(gbsph_radix_sort_s* h, size_t n) {
+    if (h->tmp_cap >= n) return GBSPH_OK;
+    if (h->tmp) cudaFree(h->tmp);
+    h->tmp = nullptr;
+    h->tmp_cap = 0;
+    if (cudaMalloc(&h->tmp, 4 * n * sizeof(uint32_t)) != cudaSuccess)
+        return fail(&h->last_error, GBSPH_ERR_OUT_OF_MEMORY, "radix sort: temporary allocation failed");
+    h->tmp_cap = n;
+    return GBSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GBSPH_API int gbsph_radix_sort_create(gbsph_radix_sort_t* out) {
+    if (!out) return GBSPH_ERR_ARGUMENT;
+    *out = nullptr;
+    auto* h = new gbsph_radix_sort_s();
+    if (cudaGetDevice(&h->device) != cudaSuccess || cudaMalloc(&h->err, 256) != cudaSuccess ||
+        cudaMemset(h->err, 0, 256) != cudaSuccess) {
+        cudaGetLastError();
+        if (h->err) cudaFree(h->err);
+        delete h;
+        return GBSPH_ERR_CUDA;
+    }
+    *out = h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_radix_sort_destroy(gbsph_radix_sort_t h) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (h->scratch) cudaFree(h->scratch);
+    if (h->tmp) cudaFree(h->tmp);
+    if (h->err) cudaFree(h->err);
+    delete h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_radix_sort_compute(gbsph_radix_sort_t h, uint32_t* keys, uint32_t* values,
+                                       size_t n_keys, size_t n_values, int start_bit,
+                                       int end_bit, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    // Checks in the reference's order (libCL/sort/oclRadixSort.cpp:64-80).
+    if (n_keys != n_values)
+        return fail(&h->last_error, GBSPH_ERR_SIZE_MISMATCH,
+                    "key and value arrays are of different size (" + std::to_string(n_keys) + "," +
+                        std::to_string(n_values) + ")");
+    if (n_keys > SORT_MAX_KEYS - SORT_TILE)
+        return fail(&h->last_error, GBSPH_ERR_TOO_LARGE,
+                    "maximum sortable array size = " + std::to_string(SORT_MAX_KEYS - SORT_TILE));
+    if (start_bit < 0 || end_bit > 32 || end_bit < start_bit || (end_bit - start_bit) % 4 != 0)
+        return fail(&h->last_error, GBSPH_ERR_BIT_RANGE,
+                    "end bit(" + std::to_string(end_bit) + ") - start bit(" + std::to_string(start_bit) +
+                        ") must be divisible by 4");
+    if (n_keys == 0 || start_bit == end_bit) return GBSPH_OK;
+    if (!keys || !values) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null key or value pointer");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    const uint32_t n = (uint32_t)n_keys;
+    const int P = sort_passes(start_bit, end_bit);
+    int rc = fit_scratch(h, onesweep_scratch_bytes(n, P));
+    if (rc) return rc;
+    rc = fit_tmp(h, n);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_prepare(h->scratch, n, P, s));
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_histogram(keys, n, start_bit, end_bit, h->scratch, s));
+    OnesweepArgs a;
+    a.keys_in = keys;
+    a.vals_in = values;
+    a.tmp_keys[0] = h->tmp;
+    a.tmp_vals[0] = h->tmp + h->tmp_cap;
+    a.tmp_keys[1] = h->tmp + 2 * h->tmp_cap;
+    a.tmp_vals[1] = h->tmp + 3 * h->tmp_cap;
+    a.n = n;
+    a.start_bit = start_bit;
+    a.end_bit = end_bit;
+    a.scratch = h->scratch;
+    a.err = h->err;
+    if (P == 1) {  // single pass cannot be in place: sort into tmp, copy back
+        a.keys_out = a.tmp_keys[0];
+        a.vals_out = a.tmp_vals[0];
+        GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(keys, a.keys_out, n * 4ull, cudaMemcpyDeviceToDevice, s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(values, a.vals_out, n * 4ull, cudaMemcpyDeviceToDevice, s));
+    } else {  // keys -> T0 -> T1 -> ... -> keys: the input is free after pass 0
+        a.keys_out = keys;
+        a.vals_out = values;
+        GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
+    }
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_radix_sort_cell_bounds(gbsph_radix_sort_t h, const uint32_t* sorted_keys,
+                                           size_t n, uint32_t* cell_start, uint32_t* cell_end,
+                                           size_t n_cells, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!cell_start || !cell_end || (n && !sorted_keys))
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null pointer");
+    if (n > 0xFFFFFFFEull || n_cells > 0xFFFFFFFFull)
+        return fail(&h->last_error, GBSPH_ERR_TOO_LARGE, "cell bounds: n or n_cells too large");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    GBSPH_CUDA_TRY(&h->last_error, cell_bounds_launch(sorted_keys, (uint32_t)n, cell_start, cell_end,
+                                                      (uint32_t)n_cells, h->err, (cudaStream_t)stream));
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t bits = 0;
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemcpy(&bits, h->err, 4, cudaMemcpyDeviceToHost));
+    if (bits) {
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->err, 0, 4));
+        return fail(&h->last_error, dev_err_to_status(bits),
+                    "device error word 0x" + std::to_string(bits));
+    }
+    return GBSPH_OK;
+}
+
+GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h) {
+    return h ? h->last_error.c_str() : "null handle";
+}
+
+}  // extern "C"

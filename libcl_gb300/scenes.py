@@ -1,0 +1,141 @@
+"""Seeded synthetic scenes for the SPH step (host numpy arrays, float4 per particle).
+
+The reference has no datasets; these generators build the jittered lattices its
+configurations describe. All randomness comes from `SplitMix64` (a published 64-bit
+generator, Steele et al. 2014) so that the same seed gives the same scene on x86 and Arm.
+"""
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import Fluid3DParams, KEY_LINEAR_GRID, params_derive
+
+_M64 = (1 << 64) - 1
+
+
+class SplitMix64:
+    """SplitMix64 stream; uniform() maps the top 24 bits to [0, 1)."""
+
+    def __init__(self, seed: int):
+        self.state = np.uint64(seed & _M64)
+
+    def next_u64(self, n: int) -> np.ndarray:
+        with np.errstate(over="ignore"):
+            idx = np.arange(1, n + 1, dtype=np.uint64)
+            z = self.state + idx * np.uint64(0x9E3779B97F4A7C15)
+            self.state = self.state + np.uint64(n) * np.uint64(0x9E3779B97F4A7C15)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            return z ^ (z >> np.uint64(31))
+
+    def uniform(self, n: int) -> np.ndarray:
+        return (self.next_u64(n) >> np.uint64(40)).astype(np.float64) / float(1 << 24)
+
+    def normal(self, n: int) -> np.ndarray:
+        """Box-Muller on pairs of uniforms."""
+        m = (n + 1) // 2
+        u1 = np.maximum(self.uniform(m), 1.0 / (1 << 25))
+        u2 = self.uniform(m)
+        r = np.sqrt(-2.0 * np.log(u1))
+        z = np.concatenate([r * np.cos(2 * np.pi * u2), r * np.sin(2 * np.pi * u2)])
+        return z[:n]
+
+
+@dataclasses.dataclass
+class Scene3D:
+    name: str
+    pos: np.ndarray      # float32 [N, 4]
+    vel: np.ndarray      # float32 [N, 4]
+    params: Fluid3DParams
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+
+def lattice(nx: int, ny: int, nz: int, spacing: float, origin, jitter: float, seed: int) -> np.ndarray:
+    """Jittered lattice, x fastest; float32 [nx*ny*nz, 4] with w = 0."""
+    iz, iy, ix = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    p = np.stack([ix.ravel(), iy.ravel(), iz.ravel()], axis=1).astype(np.float64) * spacing
+    p += np.asarray(origin, dtype=np.float64)[None, :]
+    rng = SplitMix64(seed)
+    p += (rng.uniform(p.size).reshape(p.shape) * 2.0 - 1.0) * jitter
+    out = np.zeros((p.shape[0], 4), dtype=np.float32)
+    out[:, :3] = p
+    return out
+
+
+def fluid_params(h: float, spacing: float, mass: float, rho0: float, stiffness: float,
+                 viscosity: float, dt: float, gravity, box_min, box_max, grid_dim,
+                 grid_origin=(0.0, 0.0, 0.0), dims: int = 3, velocity_limit: float = 500.0) -> Fluid3DParams:
+    p = Fluid3DParams()
+    p.deltaTime = dt
+    p.particleRadius = 0.5 * spacing
+    p.cellSize = h
+    p.mass = mass
+    p.viscosity = viscosity
+    p.pressure = 0.0
+    p.density = rho0
+    p.spacing = spacing
+    p.stiffness = stiffness
+    p.velocitylimit = velocity_limit
+    p.dims = dims
+    params_derive(p)
+    for i in range(3):
+        p.gravity[i] = gravity[i]
+        p.boxMin[i] = box_min[i]
+        p.boxMax[i] = box_max[i]
+        p.gridOrigin[i] = grid_origin[i]
+        p.gridDim[i] = grid_dim[i]
+    p.keyMode = KEY_LINEAR_GRID
+    return p
+
+
+def block_collapse_3d(nx: int = 128, ny: int = 64, nz: int = 128, seed: int = 2) -> Scene3D:
+    """3D block collapse: nx*ny*nz particles (default 1,048,576) on a lattice of spacing 0.5h
+    (h = 0.02), jittered by uniform +-0.05h, resting in the corner of a [0,4]x[0,2]x[0,4]
+    box; gravity -9.81 along y, rest density 1000, gas constant 3.0, viscosity 0.05,
+    dt = 5e-5, 200x100x200 linear cell grid. The particle mass, rho0*(0.5h)^3 = 1e-3, is a
+    choice of this generator (the configuration does not give it)."""
+    h, sp = 0.02, 0.01
+    pos = lattice(nx, ny, nz, sp, (0.5 * sp, 0.5 * sp, 0.5 * sp), 0.05 * h, seed)
+    vel = np.zeros_like(pos)
+    prm = fluid_params(h, sp, 1000.0 * sp ** 3, 1000.0, 3.0, 0.05, 5e-5, (0.0, -9.81, 0.0),
+                       (0.0, 0.0, 0.0), (4.0, 2.0, 4.0), (200, 100, 200))
+    return Scene3D(f"block_collapse_{nx}x{ny}x{nz}", pos, vel, prm)
+
+
+def dam_break_2d(nx: int = 128, ny: int = 128, seed: int = 1) -> Scene3D:
+    """2D dam break: 128x128 particles (spacing 0.5h, h = 0.01) jittered +-0.05h, anchored at
+    the lower-left corner of a [0,1]x[0,1] box; gravity -9.81, rest density 1000, gas constant
+    3.0, viscosity 0.1, dt = 1e-4, 100x100 cell grid. Mass rho0*(0.5h)^2 = 0.025 (generator's
+    choice). The 128x128 block at spacing 0.005 spans 0.64 x 0.64, more than the left quarter
+    of the box that the configuration names, so it is anchored at the wall instead."""
+    h, sp = 0.01, 0.005
+    pos = lattice(nx, ny, 1, sp, (0.5 * sp, 0.5 * sp, 0.0), 0.05 * h, seed)
+    pos[:, 2] = 0.0
+    vel = np.zeros_like(pos)
+    prm = fluid_params(h, sp, 1000.0 * sp ** 2, 1000.0, 3.0, 0.1, 1e-4, (0.0, -9.81, 0.0),
+                       (0.0, 0.0, -1.0), (1.0, 1.0, 1.0), (100, 100, 1), dims=2)
+    return Scene3D(f"dam_break_2d_{nx}x{ny}", pos, vel, prm)
+
+
+def reference_test_scene(n: int = 256, seed: int = 7) -> Scene3D:
+    """The reference's smoke scene (libCL/TEST/main.cpp:188-240): n particles uniform in
+    [-0.5, 0.5]^3 with the default parameters of clInitFluid and the reference hash keys.
+    (The reference draws from rand(); here the seeded SplitMix64 stands in.)"""
+    from . import default_params
+    rng = SplitMix64(seed)
+    pos = np.zeros((n, 4), dtype=np.float32)
+    pos[:, :3] = (rng.uniform(3 * n).reshape(n, 3) - 0.5).astype(np.float32)
+    vel = np.zeros_like(pos)
+    return Scene3D(f"reference_smoke_{n}", pos, vel, default_params())
+
+
+def clone_params(p: Fluid3DParams) -> Fluid3DParams:
+    q = Fluid3DParams()
+    import ctypes
+    ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(Fluid3DParams))
+    return q

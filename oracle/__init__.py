@@ -1,0 +1,199 @@
+"""CPU oracle for the SPH step and radix sort -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings to `oracle/_build/liboracle.so`, the C++ restatement of the reference's
+OpenCL kernels (oracle/oracle3d.cpp; each function there cites the libCL file:line it
+follows). Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+package, as the checker or the timed CPU baseline; the product library never does.
+
+Parity status: unpinned against executed reference output (the reference's OpenCL kernels
+cannot run in this environment and its tests hold no golden vectors); see the header of
+oracle3d.cpp.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "liboracle.so"
+_lib = None
+
+
+def _ensure_built() -> None:
+    if not LIB_PATH.exists():
+        import sys
+        sys.path.insert(0, str(_HERE.parent))
+        from libcl_gb300.build import build_oracle
+        build_oracle()
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _ensure_built()
+        _lib = C.CDLL(str(LIB_PATH))
+        P = C.c_void_p
+        U = C.c_uint32
+        sig = {
+            "orc_radix_sort_reference": (C.c_int, [P, P, U, U, C.c_int, C.c_int]),
+            "orc_stable_sort": (C.c_int, [P, P, U, C.c_int, C.c_int]),
+            "orc_find_bounds": (C.c_int, [P, U, P, P, U]),
+            "orc_init_fluid_params": (None, [P]),
+            "orc_hash": (None, [P, U, P, P, P]),
+            "orc_reorder": (None, [P, P, P, P, P, U]),
+            "orc_density": (None, [P, P, P, P, U, P]),
+            "orc_forces": (None, [P, P, P, P, P, P, U, P]),
+            "orc_clip_box": (None, [P, P, P, P, U, P]),
+            "orc_integrate_force": (None, [P, P, U, P]),
+            "orc_gravity": (None, [P, U, P]),
+            "orc_integrate_velocity": (None, [P, P, U, P]),
+            "orc_density_f64": (None, [P, P, P, P, P, U, P]),
+            "orc_forces_f64": (None, [P, P, P, P, P, P, P, U, P]),
+            "orc_step": (C.c_int, [P, P, P, U, P, P, P, P, P, P, P, C.c_int]),
+            "orc_step_f64": (C.c_int, [P, P, P, P, U, P, P, P, P, P, P, P]),
+            "orc_num_threads": (C.c_int, []),
+            "orc_set_num_threads": (None, [C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(_lib, name)
+            f.restype, f.argtypes = res, args
+    return _lib
+
+
+def _p(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+def _pp(params) -> int:
+    return C.addressof(params)
+
+
+def radix_sort_reference(keys: np.ndarray, vals: np.ndarray, start: int, end: int) -> int:
+    """Restated oclRadixSort (4-bit passes of 256-item blocks), in place on uint32 arrays."""
+    return lib().orc_radix_sort_reference(_p(keys), _p(vals), keys.size, vals.size, start, end)
+
+
+def stable_sort(keys: np.ndarray, vals: np.ndarray, start: int, end: int) -> None:
+    rc = lib().orc_stable_sort(_p(keys), _p(vals), keys.size, start, end)
+    assert rc == 0
+
+
+def find_bounds(sorted_keys: np.ndarray, n_cells: int):
+    cs = np.empty(n_cells, dtype=np.uint32)
+    ce = np.empty(n_cells, dtype=np.uint32)
+    lib().orc_find_bounds(_p(sorted_keys), sorted_keys.size, _p(cs), _p(ce), n_cells)
+    return cs, ce
+
+
+def init_fluid_params(params) -> None:
+    lib().orc_init_fluid_params(_pp(params))
+
+
+def table_cells(params) -> int:
+    if params.keyMode == 1:
+        return params.gridDim[0] * params.gridDim[1] * (1 if params.dims == 2 else params.gridDim[2])
+    return 262144
+
+
+class StepResult:
+    """Everything one reference step leaves behind."""
+
+    def __init__(self, n: int, cells: int):
+        self.cell = np.empty(n, np.uint32)
+        self.index = np.empty(n, np.uint32)
+        self.spos = np.empty((n, 4), np.float32)
+        self.svel = np.empty((n, 4), np.float32)
+        self.cell_start = np.empty(cells, np.uint32)
+        self.cell_end = np.empty(cells, np.uint32)
+
+
+def step(pos: np.ndarray, vel: np.ndarray, force: np.ndarray, params, ref_sort: bool = False) -> StepResult:
+    """One FP32 step of oclFluid3D::compute on host arrays (pos/vel/force updated in place)."""
+    n = pos.shape[0]
+    r = StepResult(n, table_cells(params))
+    rc = lib().orc_step(_p(pos), _p(vel), _p(force), n, _pp(params), _p(r.cell), _p(r.index),
+                        _p(r.spos), _p(r.svel), _p(r.cell_start), _p(r.cell_end), int(ref_sort))
+    assert rc == 0, rc
+    return r
+
+
+def step_f64(pos64: np.ndarray, vel64: np.ndarray, force64: np.ndarray, params):
+    """One FP64 step; keys from the positions rounded to FP32 (shared permutation)."""
+    n = pos64.shape[0]
+    fpos = pos64.astype(np.float32)
+    r = StepResult(n, table_cells(params))
+    r.spos = np.empty((n, 4), np.float64)
+    r.svel = np.empty((n, 4), np.float64)
+    rc = lib().orc_step_f64(_p(pos64), _p(vel64), _p(force64), _p(fpos), n, _pp(params), _p(r.cell),
+                            _p(r.index), _p(r.spos), _p(r.svel), _p(r.cell_start), _p(r.cell_end))
+    assert rc == 0, rc
+    return r
+
+
+def density(spos, svel, cs, ce, params):
+    lib().orc_density(_p(spos), _p(svel), _p(cs), _p(ce), spos.shape[0], _pp(params))
+
+
+def forces(spos, svel, force, index, cs, ce, params):
+    lib().orc_forces(_p(spos), _p(svel), _p(force), _p(index), _p(cs), _p(ce), spos.shape[0], _pp(params))
+
+
+def density_f64(spos64, svel64, fspos, cs, ce, params):
+    lib().orc_density_f64(_p(spos64), _p(svel64), _p(fspos), _p(cs), _p(ce), spos64.shape[0], _pp(params))
+
+
+def forces_f64(spos64, svel64, force64, index, fspos, cs, ce, params):
+    lib().orc_forces_f64(_p(spos64), _p(svel64), _p(force64), _p(index), _p(fspos), _p(cs), _p(ce),
+                         spos64.shape[0], _pp(params))
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def set_num_threads(n: int) -> None:
+    lib().orc_set_num_threads(n)
+
+
+def hash(pos, params):
+    n = pos.shape[0]
+    cell = np.empty(n, np.uint32)
+    index = np.empty(n, np.uint32)
+    lib().orc_hash(_p(pos), n, _pp(params), _p(cell), _p(index))
+    return cell, index
+
+
+def reorder(index, pos, vel):
+    n = pos.shape[0]
+    spos = np.empty_like(pos)
+    svel = np.empty_like(vel)
+    lib().orc_reorder(_p(index), _p(pos), _p(vel), _p(spos), _p(svel), n)
+    return spos, svel
+
+
+def clip_box(spos, svel, force, index, params):
+    lib().orc_clip_box(_p(spos), _p(svel), _p(force), _p(index), spos.shape[0], _pp(params))
+
+
+def integrate_force(vel, force, params):
+    lib().orc_integrate_force(_p(vel), _p(force), vel.shape[0], _pp(params))
+
+
+def gravity(force, params):
+    lib().orc_gravity(_p(force), force.shape[0], _pp(params))
+
+
+def integrate_velocity(pos, vel, params):
+    lib().orc_integrate_velocity(_p(pos), _p(vel), pos.shape[0], _pp(params))
+
+
+def front_end(pos, vel, params):
+    """hash -> stable sort on bits [0,24) -> reorder -> fill + find bounds."""
+    cell, index = hash(pos, params)
+    stable_sort(cell, index, 0, 24)
+    spos, svel = reorder(index, pos, vel)
+    cs, ce = find_bounds(cell, table_cells(params))
+    return cell, index, spos, svel, cs, ce

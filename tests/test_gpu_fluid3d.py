@@ -1,0 +1,263 @@
+"""GPU parity of the 3D SPH step against the oracle (the FP32 restatement of oclFluid3D.cl),
+driven through the C ABI. Keys, sorted permutation and cell bounds are bit-exact everywhere;
+the exact (reference-order) kernels are bit-exact for density, force and state as well; the
+fast brick kernels agree within RTOL (tests/fluid_helpers.py)."""
+import numpy as np
+import pytest
+
+import oracle
+from fluid_helpers import RTOL, hash_block, make_fluid, perturbed, rel_err, set_params, sorted_outputs, state
+from libcl_gb300 import (ERR_ARGUMENT, ERR_NOT_COMPILED, ERR_SIZE_MISMATCH, OK, OPT_BRICK_WIDTH, REF_BUCKETS,
+                         STAGE_GRAVITY, STAGE_INTEGRATE_FORCE, STAGE_INTEGRATE_VELOCITY, Fluid3D)
+from libcl_gb300.scenes import block_collapse_3d, clone_params, reference_test_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def assert_bit_exact(a, b, what):
+    ba, bb = bits(a), bits(b)
+    if not np.array_equal(ba, bb):
+        bad = np.argwhere(ba != bb)
+        raise AssertionError(f"{what}: {len(bad)} entries differ, first at {bad[0]}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}")
+
+
+def oracle_step(scene, vel, force=None, ref_sort=False):
+    pos = scene.pos.copy()
+    v = vel.copy()
+    f = np.zeros_like(scene.pos) if force is None else force.copy()
+    r = oracle.step(pos, v, f, scene.params, ref_sort=ref_sort)
+    return r, {"pos": pos, "vel": v, "force": f}
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_hash_mode_step_bit_exact(cuda, fused):
+    """REFERENCE_HASH keys (262144 buckets, duplicate bucket visits included): everything
+    bit-exact against the restatement, including density, pressure, force and state."""
+    sc = hash_block(24)
+    vel = perturbed(sc)
+    f = make_fluid(sc, fused=fused, vel=vel)
+    f.compute()
+    g, gs = sorted_outputs(f, REF_BUCKETS), state(f)
+    r, rs = oracle_step(sc, vel, ref_sort=True)
+    assert_bit_exact(g["cell"], r.cell, "keys")
+    assert_bit_exact(g["index"], r.index, "index")
+    assert_bit_exact(g["cell_start"], r.cell_start, "cellStart")
+    assert_bit_exact(g["cell_end"], r.cell_end, "cellEnd")
+    assert_bit_exact(g["spos"], r.spos, "sorted position (.w = density)")
+    assert_bit_exact(g["svel"], r.svel, "sorted velocity (.w = pressure)")
+    for k in ("pos", "vel", "force"):
+        assert_bit_exact(gs[k], rs[k], k)
+    assert f.sync_status() == OK
+
+
+def test_linear_staged_step_bit_exact(cuda):
+    sc = block_collapse_3d(32, 16, 32)
+    vel = perturbed(sc)
+    f = make_fluid(sc, fused=False, vel=vel)
+    f.compute()
+    g, gs = sorted_outputs(f, oracle.table_cells(sc.params)), state(f)
+    r, rs = oracle_step(sc, vel)
+    for k, rv in (("cell", r.cell), ("index", r.index), ("cell_start", r.cell_start), ("cell_end", r.cell_end),
+                  ("spos", r.spos), ("svel", r.svel)):
+        assert_bit_exact(g[k], rv, k)
+    for k in ("pos", "vel", "force"):
+        assert_bit_exact(gs[k], rs[k], k)
+
+
+def compare_fast(g, gs, r, rs, prev_pos, tol=RTOL):
+    """Fast path: integer outputs exact, float outputs within tol."""
+    assert_bit_exact(g["cell"], r.cell, "keys")
+    assert_bit_exact(g["index"], r.index, "index")
+    assert_bit_exact(g["cell_start"], r.cell_start, "cellStart")
+    assert_bit_exact(g["cell_end"], r.cell_end, "cellEnd")
+    assert_bit_exact(g["spos"][:, :3], r.spos[:, :3], "sorted position xyz")
+    assert_bit_exact(g["svel"][:, :3], r.svel[:, :3], "sorted velocity xyz")
+    errs = {
+        "density": rel_err(g["spos"][:, 3], r.spos[:, 3]),
+        "pressure": rel_err(g["svel"][:, 3], r.svel[:, 3]),
+        "velocity": rel_err(gs["vel"], rs["vel"]),
+        "displacement": rel_err(gs["pos"] - prev_pos, rs["pos"] - prev_pos),
+    }
+    assert_bit_exact(gs["force"], rs["force"], "force (gravity seed)")
+    for k, e in errs.items():
+        assert e <= tol, f"{k}: relative error {e:.3e} > {tol:.1e}"
+    return errs
+
+
+def test_linear_fused_step_within_tolerance(cuda):
+    sc = block_collapse_3d(64, 32, 64)
+    vel = perturbed(sc)
+    f = make_fluid(sc, fused=True, vel=vel)
+    f.compute()
+    g, gs = sorted_outputs(f, oracle.table_cells(sc.params)), state(f)
+    r, rs = oracle_step(sc, vel)
+    errs = compare_fast(g, gs, r, rs, sc.pos)
+    print("fused-vs-restatement relative errors:", errs)
+    assert f.sync_status() == OK
+
+
+def test_linear_fused_steps_fed_identical_state(cuda):
+    """Several steps; before each, the oracle is fed the GPU's own prior state (trajectories
+    are chaotic, so single steps are compared, not long runs)."""
+    sc = block_collapse_3d(48, 24, 48)
+    vel = perturbed(sc, sigma=0.2)
+    f = make_fluid(sc, fused=True, vel=vel)
+    cells = oracle.table_cells(sc.params)
+    for step in range(4):
+        before = state(f)
+        f.compute()
+        g, gs = sorted_outputs(f, cells), state(f)
+        pos, v, frc = before["pos"].copy(), before["vel"].copy(), before["force"].copy()
+        r = oracle.step(pos, v, frc, sc.params)
+        compare_fast(g, gs, r, {"pos": pos, "vel": v, "force": frc}, before["pos"])
+
+
+def test_graph_replay_equals_eager(cuda):
+    sc = block_collapse_3d(32, 16, 32)
+    vel = perturbed(sc)
+    a = make_fluid(sc, fused=True, graph=True, vel=vel)
+    b = make_fluid(sc, fused=True, graph=False, vel=vel)
+    for _ in range(5):
+        a.compute()
+        b.compute()
+    sa, sb = state(a), state(b)
+    for k in sa:
+        assert_bit_exact(sa[k], sb[k], k)
+
+
+@pytest.mark.parametrize("bw", [1, 3, 16])
+def test_brick_width_does_not_change_results(cuda, bw):
+    """Each target's candidate order depends only on its own neighbourhood, not on how cells
+    are grouped into bricks."""
+    sc = block_collapse_3d(32, 16, 32)
+    vel = perturbed(sc)
+    a = make_fluid(sc, vel=vel)
+    b = make_fluid(sc, vel=vel)
+    b.set_option(OPT_BRICK_WIDTH, bw)
+    a.compute()
+    b.compute()
+    sa, sb = state(a), state(b)
+    for k in sa:
+        assert_bit_exact(sa[k], sb[k], k)
+
+
+def test_integrate_hook(cuda):
+    """EVT_INTEGRATE as in libCL/TEST/main.cpp:246-343: the handler runs integrate-force,
+    gravity and integrate-velocity itself and skips the clip box."""
+    sc = hash_block(16)
+    vel = perturbed(sc)
+    f = make_fluid(sc, fused=True, vel=vel)
+    calls = []
+
+    def handler(fluid, stream):
+        calls.append(1)
+        for st in (STAGE_INTEGRATE_FORCE, STAGE_GRAVITY, STAGE_INTEGRATE_VELOCITY):
+            fluid.stage(st, stream)
+        return 0
+
+    f.addEventHandler(handler)
+    f.compute()
+    gs = state(f)
+    assert calls == [1]
+    p = sc.params
+    pos, v, frc = sc.pos.copy(), vel.copy(), np.zeros_like(sc.pos)
+    cell, index, spos, svel, cs, ce = oracle.front_end(pos, v, p)
+    oracle.density(spos, svel, cs, ce, p)
+    oracle.forces(spos, svel, frc, index, cs, ce, p)
+    oracle.integrate_force(v, frc, p)
+    oracle.gravity(frc, p)
+    oracle.integrate_velocity(pos, v, p)
+    for k, rv in (("pos", pos), ("vel", v), ("force", frc)):
+        assert_bit_exact(gs[k], rv, k)
+
+
+def test_hook_failure_is_reported(cuda):
+    sc = hash_block(8)
+    f = make_fluid(sc)
+    f.addEventHandler(lambda fluid, stream: 3)
+    from libcl_gb300 import ERR_STATE
+    assert f.compute_raw() == ERR_STATE
+    assert "hook" in f.last_error()
+
+
+def test_reference_smoke_scene_runs(cuda):
+    """The reference's own smoke run (256 particles, defaults): a few steps stay finite and
+    particle 0 matches the restatement after one step."""
+    sc = reference_test_scene(256)
+    f = make_fluid(sc)
+    f.compute()
+    gs = state(f)
+    r, rs = oracle_step(sc, sc.vel, ref_sort=True)
+    for k in ("pos", "vel", "force"):
+        assert_bit_exact(gs[k], rs[k], k)
+    for _ in range(20):
+        f.compute()
+    assert np.isfinite(state(f)["pos"]).all()
+
+
+def test_errors_and_validation(cuda):
+    import torch
+    f = Fluid3D()
+    assert f.compute_raw() == ERR_NOT_COMPILED
+    f.compile()
+    assert f.compute_raw() == OK
+    p = f.getParameters()
+    saved = clone_params(p)
+    p.cellSize = float("nan")
+    assert f.compute_raw() == ERR_ARGUMENT
+    set_params(f, saved)
+    p.keyMode = 1
+    p.gridDim[0] = 0
+    assert f.compute_raw() == ERR_ARGUMENT
+    set_params(f, saved)
+    n = f.getParticleCount()
+    assert n == 256
+    bad = torch.zeros((n + 1, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(Exception) as e:
+        f.setPositionBuffer(bad)
+    assert e.value.status == ERR_SIZE_MISMATCH
+    ok = torch.zeros((n + 8, 4), dtype=torch.float32, device="cuda")
+    f.setVelocityBuffer(ok)  # velocity/force accept count >= N
+    with pytest.raises(Exception):
+        f.set_option(OPT_BRICK_WIDTH, 0)
+    with pytest.raises(Exception) as e:
+        f.setParticleCount(n + 100)  # the borrowed velocity buffer is too small
+    assert e.value.status == ERR_SIZE_MISMATCH
+    assert f.compute_raw() == OK
+    torch.cuda.synchronize()
+
+
+def test_borrowed_buffers(cuda):
+    """setPositionBuffer/setVelocityBuffer with caller-owned memory (never freed by the fluid)."""
+    import torch
+    sc = block_collapse_3d(16, 8, 16)
+    f = make_fluid(sc)
+    pos = torch.from_numpy(sc.pos).cuda()
+    vel = torch.zeros_like(pos)
+    f.setPositionBuffer(pos)
+    f.setVelocityBuffer(vel)
+    f.compute()
+    torch.cuda.synchronize()
+    assert f.getPositionBuffer().data_ptr() == pos.data_ptr()
+    assert not torch.equal(pos.cpu(), torch.from_numpy(sc.pos))  # moved in place
+    del f
+    torch.cuda.synchronize()
+    assert torch.isfinite(pos).all()  # still valid memory after the fluid is gone
+
+
+def test_c2_full_size_one_step(cuda):
+    """1,048,576 particles, 200x100x200 grid: one fused step against the restatement."""
+    sc = block_collapse_3d()
+    f = make_fluid(sc, fused=True)
+    f.compute()
+    g, gs = sorted_outputs(f, oracle.table_cells(sc.params)), state(f)
+    idx = g["index"]
+    assert np.array_equal(np.sort(idx), np.arange(sc.n, dtype=np.uint32))
+    assert np.all(g["cell"][1:] >= g["cell"][:-1])
+    r, rs = oracle_step(sc, sc.vel)
+    errs = compare_fast(g, gs, r, rs, sc.pos)
+    print("C2 1M fused-vs-restatement relative errors:", errs)
