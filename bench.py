@@ -203,6 +203,7 @@ def main(argv=None) -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--quick", action="store_true", help="skip e2e/profile/baseline legs (for ncu)")
+    ap.add_argument("--brick-width", type=int, default=0, help="cells per neighbour brick (0: library default)")
     args = ap.parse_args(argv)
     rank, world, local = env_rank()
     if args.impl == "reference":
@@ -222,6 +223,9 @@ def main(argv=None) -> int:
     scene = block_collapse_3d()
     fluid = Fluid3D()
     load_scene(fluid, scene)
+    if args.brick_width:
+        from libcl_gb300 import OPT_BRICK_WIDTH
+        fluid.set_option(OPT_BRICK_WIDTH, args.brick_width)
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 

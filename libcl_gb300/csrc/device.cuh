@@ -7,9 +7,30 @@
 
 namespace gbsph {
 
-// Bounded waits: after this many polls a kernel gives up, sets an error bit and moves on.
-// With the back-off below that is well under a second on a GB300.
-constexpr uint32_t SPIN_LIMIT = 1u << 22;
+// Bounded waits: a kernel that has polled for WAIT_LIMIT_NS of wall-clock time (read from
+// %globaltimer every 32 polls) gives up, sets an error bit and moves on.
+constexpr uint64_t WAIT_LIMIT_NS = 1000000000ull;
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Poll-loop guard: call once per poll; returns true once the wait has lasted too long.
+struct WaitBudget {
+    uint64_t start = 0;
+    uint32_t polls = 0;
+    __device__ __forceinline__ bool expired() {
+        if ((++polls & 31u) != 0u) return false;
+        const uint64_t now = globaltimer_ns();
+        if (start == 0) {
+            start = now;
+            return false;
+        }
+        return now - start > WAIT_LIMIT_NS;
+    }
+};
 
 __device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* p) {
     uint32_t v;
@@ -79,11 +100,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait on phase `parity`. Returns false if the limit was reached.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < SPIN_LIMIT; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (i > 16) __nanosleep(64);
+    WaitBudget budget;
+    while (!mbar_try_wait(bar, parity)) {
+        if (budget.expired()) return false;
     }
-    return false;
+    return true;
 }
 
 // ---- float4 helpers ---------------------------------------------------------------------

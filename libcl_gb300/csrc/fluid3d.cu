@@ -703,7 +703,9 @@ GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream) {
     h->table_clean = false;
     switch (stage) {
         case GBSPH_STAGE_HASH: return st_hash(h, kp, s, false);
-        case GBSPH_STAGE_SORT: return st_sort(h, kp, s, false);
+        case GBSPH_STAGE_SORT:
+            GBSPH_CUDA_TRY(&h->last_error, onesweep_reset_progress(h->scratch, kp.n, sort_passes(0, kp.end_bit), s));
+            return st_sort(h, kp, s, false);
         case GBSPH_STAGE_REORDER: return st_reorder(h, kp, s);
         case GBSPH_STAGE_BOUNDS: return st_bounds(h, kp, s, true);
         case GBSPH_STAGE_DENSITY: return st_density_exact(h, kp, s);

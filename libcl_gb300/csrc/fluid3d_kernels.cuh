@@ -382,7 +382,8 @@ struct BrickShared {
 // Returns the brick's first cell x and cell count through x0/ncell.
 template <int DIMS>
 __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, uint32_t bid,
-                                            const uint2* __restrict__ table, int& x0, int& ncell) {
+                                            const uint2* __restrict__ table, uint32_t* err, int& x0,
+                                            int& ncell) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     const int W = kp.bw;
     const int bx = (int)(bid % (uint32_t)kp.bxn);
@@ -418,8 +419,15 @@ __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, u
                 acc += S.cnt[t][c];
             }
         }
+        if (lo == EMPTY) lo = 0;
+        if ((uint64_t)lo + acc > kp.n) {  // inconsistent table: report, use an empty row
+            atomicOr(err, DEV_ERR_KEY_RANGE);
+            for (int c = 0; c < W + 2; ++c) S.off[t][c] = 0;
+            acc = 0;
+            lo = 0;
+        }
         S.off[t][W + 2] = acc;
-        S.lo[t] = lo == EMPTY ? 0u : lo;
+        S.lo[t] = lo;
         S.rcnt[t] = acc;
     }
     __syncthreads();
@@ -503,7 +511,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
         int x0, ncell;
-        brick_setup<DIMS>(S, kp, bricks[b], table, x0, ncell);
+        brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
         const bool staged = brick_stage<DIMS, 1>(S, s_buf, cap, spos, nullptr);
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
@@ -586,7 +594,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
         int x0, ncell;
-        brick_setup<DIMS>(S, kp, bricks[b], table, x0, ncell);
+        brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
         const bool staged = brick_stage<DIMS, 2>(S, s_buf, cap, spos, svel);
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
@@ -619,7 +627,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                                 const float inv = rsqrtf(r2);
                                 const float vlen = r2 * inv;
                                 const float hr = kp.h - vlen;
-                                const float dd = inv_rho_i / pj.w;           // 1/(rho_i rho_j)
+                                const float dd = inv_rho_i * __frcp_rn(pj.w);  // 1/(rho_i rho_j)
                                 const float sp = (vi.w + vj.w) * dd * hr * hr * inv;
                                 px = fmaf(sp, dx, px);
                                 py = fmaf(sp, dy, py);

@@ -84,6 +84,9 @@ struct OnesweepArgs {
 
 // Zeroes the scratch header and the look-back words.
 cudaError_t onesweep_prepare(void* scratch, uint32_t n, int passes, cudaStream_t s);
+// Zeroes only the tile counters and look-back words (keeps the histogram), so that the
+// passes can be re-run on the same keys.
+cudaError_t onesweep_reset_progress(void* scratch, uint32_t n, int passes, cudaStream_t s);
 // Histogram of every pass's digit (not needed when the caller's kernel filled hist).
 cudaError_t onesweep_histogram(const uint32_t* keys, uint32_t n, int start_bit, int end_bit,
                                void* scratch, cudaStream_t s);

@@ -102,6 +102,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     for (int i = t; i < SORT_WARPS * SORT_RADIX; i += SORT_THREADS) s_whist[i] = 0;
     __syncthreads();
     const uint32_t tile = s_tile;
+    if (tile >= tiles) {  // counter not reset since the last sort: refuse rather than overrun
+        if (t == 0) atomicOr(err, DEV_ERR_CAPACITY);
+        return;
+    }
     const uint32_t base = tile * SORT_TILE;
     const uint32_t mask = (1u << bits) - 1u;
 
@@ -159,15 +163,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     } else {
         st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_AGG | cnt);
         int pred = (int)tile - 1;
-        uint32_t spins = 0;
+        WaitBudget budget;
         while (pred >= 0) {
             const uint32_t s = ld_relaxed_gpu(&status[(size_t)pred * SORT_RADIX + t]);
             if ((s & ~COUNT_MASK) == 0u) {
-                if (++spins > SPIN_LIMIT) {
+                if (budget.expired()) {
                     atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
                     break;
                 }
-                if (spins > 32) __nanosleep(64);
                 continue;
             }
             excl += s & COUNT_MASK;
@@ -197,6 +200,10 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         if (j < valid) {
             const uint32_t key = s_keys[j], val = s_vals[j];
             const uint32_t dst = s_base[(key >> shift) & mask] + j;
+            if (dst >= n) {  // histogram inconsistent with the keys (misuse): never write out of range
+                atomicOr(err, DEV_ERR_KEY_RANGE);
+                continue;
+            }
             keys_out[dst] = key;
             vals_out[dst] = val;
             if (NGATHER > 0) gather.dst[0][dst] = __ldg(gather.src[0] + val);
@@ -248,6 +255,13 @@ size_t onesweep_scratch_bytes(uint32_t n, int passes) {
 
 cudaError_t onesweep_prepare(void* scratch, uint32_t n, int passes, cudaStream_t s) {
     return cudaMemsetAsync(scratch, 0, onesweep_scratch_bytes(n, passes), s);
+}
+
+cudaError_t onesweep_reset_progress(void* scratch, uint32_t n, int passes, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync((char*)scratch + 4096, 0, 16, s);
+    if (e != cudaSuccess) return e;
+    return cudaMemsetAsync((char*)scratch + SORT_HEADER_BYTES, 0,
+                           onesweep_scratch_bytes(n, passes) - SORT_HEADER_BYTES, s);
 }
 
 cudaError_t onesweep_histogram(const uint32_t* keys, uint32_t n, int start_bit, int end_bit,

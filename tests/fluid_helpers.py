@@ -73,6 +73,17 @@ def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.max(np.abs(a - b) / (np.abs(b) + scale)))
 
 
+def pos_err(new: np.ndarray, ref: np.ndarray, prev: np.ndarray, ulps: float = 4.0) -> float:
+    """Position check that stays meaningful when a step moves particles by less than one ulp:
+    max |new - ref| / (ulps * ulp(|ref|) + RTOL * (|ref - prev| + RMS(ref - prev))). <= 1 passes."""
+    new = np.asarray(new, np.float64)
+    ref64 = np.asarray(ref, np.float64)
+    d = ref64 - np.asarray(prev, np.float64)
+    ulp = np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
+    den = ulps * ulp + RTOL * (np.abs(d) + np.sqrt(np.mean(d * d)) + 1e-30)
+    return float(np.max(np.abs(new - ref64) / den))
+
+
 def perturbed(scene: Scene3D, seed: int = 5, sigma: float = 0.05) -> np.ndarray:
     rng = SplitMix64(seed)
     v = np.zeros_like(scene.pos)
@@ -80,5 +91,5 @@ def perturbed(scene: Scene3D, seed: int = 5, sigma: float = 0.05) -> np.ndarray:
     return v
 
 
-__all__ = ["hash_block", "make_fluid", "state", "sorted_outputs", "rel_err", "RTOL", "set_params",
+__all__ = ["hash_block", "make_fluid", "state", "sorted_outputs", "rel_err", "pos_err", "RTOL", "set_params",
            "clone_params", "perturbed"]

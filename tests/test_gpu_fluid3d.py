@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle
-from fluid_helpers import RTOL, hash_block, make_fluid, perturbed, rel_err, set_params, sorted_outputs, state
+from fluid_helpers import RTOL, hash_block, make_fluid, perturbed, pos_err, rel_err, set_params, sorted_outputs, state
 from libcl_gb300 import (ERR_ARGUMENT, ERR_NOT_COMPILED, ERR_SIZE_MISMATCH, OK, OPT_BRICK_WIDTH, REF_BUCKETS,
                          STAGE_GRAVITY, STAGE_INTEGRATE_FORCE, STAGE_INTEGRATE_VELOCITY, Fluid3D)
 from libcl_gb300.scenes import block_collapse_3d, clone_params, reference_test_scene
@@ -80,11 +80,12 @@ def compare_fast(g, gs, r, rs, prev_pos, tol=RTOL):
         "density": rel_err(g["spos"][:, 3], r.spos[:, 3]),
         "pressure": rel_err(g["svel"][:, 3], r.svel[:, 3]),
         "velocity": rel_err(gs["vel"], rs["vel"]),
-        "displacement": rel_err(gs["pos"] - prev_pos, rs["pos"] - prev_pos),
     }
     assert_bit_exact(gs["force"], rs["force"], "force (gravity seed)")
     for k, e in errs.items():
         assert e <= tol, f"{k}: relative error {e:.3e} > {tol:.1e}"
+    errs["position"] = pos_err(gs["pos"], rs["pos"], prev_pos)
+    assert errs["position"] <= 1.0, f"position: {errs['position']:.3f} x (4 ulp + RTOL * displacement)"
     return errs
 
 
