@@ -1,0 +1,234 @@
+// gbFluid3D.hpp -- header-only C++ class surface over the C ABI in gbsph.h.
+//
+// Mirrors the classes a libCL user calls for the SPH path (jochenstier/libcl):
+//   oclContext / oclDevice   (libCL/oclContext.h:25-49, libCL/oclDevice.h:22-45) -> gbContext / gbDevice
+//   oclBuffer                (libCL/oclBuffer.h:22-70, libCL/oclMem.h:22-60)      -> gbBuffer
+//   oclRadixSort             (libCL/sort/oclRadixSort.h:22-49)                     -> gbRadixSort
+//   oclFluid3D + srtEvent    (libCL/phys/oclFluid3D.h:21-123, libCL/oclProgram.h:104-116)
+//                                                                                  -> gbFluid3D + srtEvent
+// Same method names and meanings: construct, compile(), setParticleCount(), set/get buffers,
+// getParameters(), addEventHandler(EVT_INTEGRATE), compute(device), map()/unmap() to read
+// results. Methods return 1/true on success and 0/false on failure like the reference; the
+// last status code is kept in gbStatus (the reference's sStatusCL, libCL/oclCommon.cpp:19).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbsph.h"
+
+inline int& gbStatus() {
+    static thread_local int s = GBSPH_OK;
+    return s;
+}
+
+class gbDevice {
+   public:
+    explicit gbDevice(int ordinal = 0, cudaStream_t stream = nullptr) : mOrdinal(ordinal), mStream(stream) {}
+    cudaStream_t getQueue() const { return mStream; }
+    operator cudaStream_t() const { return mStream; }
+    int ordinal() const { return mOrdinal; }
+    void setQueue(cudaStream_t s) { mStream = s; }
+
+   private:
+    int mOrdinal;
+    cudaStream_t mStream;
+};
+
+class gbContext {
+   public:
+    explicit gbContext(int device = 0) : mDevice(device) { cudaSetDevice(device); }
+    gbDevice& getDevice(int) { return mDevice; }
+
+   private:
+    gbDevice mDevice;
+};
+
+// Device buffer with an owner tag; map()/unmap() stage a host copy (the reference maps
+// ALLOC_HOST_PTR buffers, libCL/oclBuffer.cpp:26-45, libCL/oclMem.cpp:64-84).
+class gbBuffer {
+   public:
+    enum { MAP_READ = 1, MAP_WRITE = 2 };
+    gbBuffer(gbContext&, const char* name) : mName(name) {}
+    ~gbBuffer() { release(); }
+    gbBuffer(const gbBuffer&) = delete;
+    gbBuffer& operator=(const gbBuffer&) = delete;
+
+    template <class T>
+    bool create(size_t count) {
+        release();
+        gbStatus() = cudaMalloc(&mPtr, count * sizeof(T)) == cudaSuccess ? GBSPH_OK : GBSPH_ERR_OUT_OF_MEMORY;
+        if (gbStatus() != GBSPH_OK) return false;
+        cudaMemset(mPtr, 0, count * sizeof(T));
+        mBytes = count * sizeof(T);
+        mOwned = true;
+        return true;
+    }
+    // Wraps memory owned elsewhere (a fluid's internal buffer); never freed by this object.
+    void wrap(void* device_ptr, size_t bytes) {
+        release();
+        mPtr = device_ptr;
+        mBytes = bytes;
+        mOwned = false;
+    }
+    template <class T>
+    size_t count() const { return mBytes / sizeof(T); }
+    size_t bytes() const { return mBytes; }
+    void* devicePtr() const { return mPtr; }
+    const std::string& getName() const { return mName; }
+    template <class T>
+    T* ptr() { return reinterpret_cast<T*>(mHost.data()); }
+    bool map(int flags) {
+        mHost.resize(mBytes);
+        mMapFlags = flags;
+        if (flags & MAP_READ) return cudaMemcpy(mHost.data(), mPtr, mBytes, cudaMemcpyDeviceToHost) == cudaSuccess;
+        return true;
+    }
+    bool unmap() {
+        bool ok = true;
+        if (mMapFlags & MAP_WRITE) ok = cudaMemcpy(mPtr, mHost.data(), mBytes, cudaMemcpyHostToDevice) == cudaSuccess;
+        mMapFlags = 0;
+        return ok;
+    }
+    void setOwner(const void* owner) { mOwner = owner; }
+    const void* getOwner() const { return mOwner; }
+
+   private:
+    void release() {
+        if (mOwned && mPtr) cudaFree(mPtr);
+        mPtr = nullptr;
+        mBytes = 0;
+        mOwned = false;
+    }
+    std::string mName;
+    void* mPtr = nullptr;
+    size_t mBytes = 0;
+    bool mOwned = false;
+    int mMapFlags = 0;
+    const void* mOwner = nullptr;
+    std::vector<unsigned char> mHost;
+};
+
+class gbRadixSort {
+   public:
+    explicit gbRadixSort(gbContext&) { gbStatus() = gbsph_radix_sort_create(&mH); }
+    ~gbRadixSort() {
+        if (mH) gbsph_radix_sort_destroy(mH);
+    }
+    int compile() { return mH != nullptr; }
+    // oclRadixSort::compute(oclDevice&, oclBuffer& key, oclBuffer& val, int startBit, int endBit)
+    int compute(gbDevice& dev, gbBuffer& key, gbBuffer& val, int startBit, int endBit) {
+        gbStatus() = gbsph_radix_sort_compute(mH, (uint32_t*)key.devicePtr(), (uint32_t*)val.devicePtr(),
+                                              key.count<uint32_t>(), val.count<uint32_t>(), startBit, endBit,
+                                              dev.getQueue());
+        return gbStatus() == GBSPH_OK;
+    }
+    const char* lastError() const { return gbsph_radix_sort_last_error(mH); }
+
+   private:
+    gbsph_radix_sort_t mH = nullptr;
+};
+
+class gbFluid3D;
+
+// Event handler (srtEvent, libCL/oclProgram.h:104-116): called by compute() in place of the
+// clip/integrate stages when registered for EVT_INTEGRATE.
+struct srtEvent {
+    explicit srtEvent(const char* name, void* data = nullptr) : mName(name), mData(data) {}
+    virtual ~srtEvent() = default;
+    virtual bool operator()(gbFluid3D& fluid) = 0;
+    const char* mName;
+    void* mData;
+};
+
+class gbFluid3D {
+   public:
+    typedef gbsph_fluid3d_params Params;
+    static constexpr const char* EVT_INTEGRATE = "OnIntegrate";
+    static constexpr size_t cLocalSize = 256;
+    static constexpr size_t cBucketCount = 262144;
+
+    explicit gbFluid3D(gbContext& ctx)
+        : mPosition(ctx, "bfPosition"), mVelocity(ctx, "bfVelocity"), mForce(ctx, "bfForce"),
+          mSortedPosition(ctx, "bfSortedPosition"), mSortedVelocity(ctx, "bfSortedVelocity"),
+          mIndex(ctx, "bfIndex") {
+        gbStatus() = gbsph_fluid3d_create(&mH);
+        rewrap();
+    }
+    ~gbFluid3D() {
+        if (mH) gbsph_fluid3d_destroy(mH);
+    }
+    gbFluid3D(const gbFluid3D&) = delete;
+    gbFluid3D& operator=(const gbFluid3D&) = delete;
+
+    int compile() { return ok(gbsph_fluid3d_compile(mH)); }
+    int compute(gbDevice& dev) {
+        mDevice = &dev;
+        return ok(gbsph_fluid3d_compute(mH, dev.getQueue()));
+    }
+    // One reference stage (GBSPH_STAGE_*), e.g. from an EVT_INTEGRATE handler.
+    int stage(int which) { return ok(gbsph_fluid3d_stage(mH, which, mDevice ? mDevice->getQueue() : nullptr)); }
+
+    void setParticleCount(size_t n) {
+        ok(gbsph_fluid3d_set_particle_count(mH, n));
+        rewrap();
+    }
+    size_t getParticleCount() { return gbsph_fluid3d_get_particle_count(mH); }
+
+    int setPositionBuffer(gbBuffer* b) { return setBuffer(GBSPH_BUF_POSITION, b); }
+    int setVelocityBuffer(gbBuffer* b) { return setBuffer(GBSPH_BUF_VELOCITY, b); }
+    int setForceBuffer(gbBuffer* b) { return setBuffer(GBSPH_BUF_FORCE, b); }
+
+    gbBuffer* getPositionBuffer() { return mUser[0] ? mUser[0] : &mPosition; }
+    gbBuffer* getVelocityBuffer() { return mUser[1] ? mUser[1] : &mVelocity; }
+    gbBuffer* getForceBuffer() { return mUser[2] ? mUser[2] : &mForce; }
+    gbBuffer& getSortedPositionBuffer() { return mSortedPosition; }
+    gbBuffer& getSortedVelocityBuffer() { return mSortedVelocity; }
+    gbBuffer& getIndexBuffer() { return mIndex; }
+
+    Params& getParameters() { return *gbsph_fluid3d_get_params(mH); }
+
+    void addEventHandler(srtEvent& e) {
+        if (std::strcmp(e.mName, EVT_INTEGRATE) != 0) return;
+        mHandler = &e;
+        gbsph_fluid3d_set_integrate_hook(mH, &gbFluid3D::hookTrampoline, this);
+    }
+    const char* lastError() const { return gbsph_fluid3d_last_error(mH); }
+    gbsph_fluid3d_t handle() const { return mH; }
+
+   private:
+    static int hookTrampoline(gbsph_fluid3d_t, void* stream, void* user) {
+        gbFluid3D* self = static_cast<gbFluid3D*>(user);
+        if (self->mDevice) self->mDevice->setQueue((cudaStream_t)stream);
+        return (*self->mHandler)(*self) ? 0 : 1;
+    }
+    int ok(int status) {
+        gbStatus() = status;
+        return status == GBSPH_OK;
+    }
+    int setBuffer(int which, gbBuffer* b) {
+        const int r = ok(gbsph_fluid3d_set_buffer(mH, which, b->devicePtr(), b->count<float>() / 4));
+        if (r) mUser[which] = b;
+        return r;
+    }
+    void rewrap() {
+        gbBuffer* own[6] = {&mPosition, &mVelocity, &mForce, &mSortedPosition, &mSortedVelocity, &mIndex};
+        const int which[6] = {GBSPH_BUF_POSITION, GBSPH_BUF_VELOCITY, GBSPH_BUF_FORCE,
+                              GBSPH_BUF_SORTED_POSITION, GBSPH_BUF_SORTED_VELOCITY, GBSPH_BUF_INDEX};
+        for (int i = 0; i < 6; i++) {
+            size_t count = 0;
+            void* p = mH ? gbsph_fluid3d_get_buffer(mH, which[i], &count) : nullptr;
+            own[i]->wrap(p, count * (which[i] == GBSPH_BUF_INDEX ? 4 : 16));
+            own[i]->setOwner(this);
+        }
+    }
+
+    gbsph_fluid3d_t mH = nullptr;
+    gbBuffer mPosition, mVelocity, mForce, mSortedPosition, mSortedVelocity, mIndex;
+    gbBuffer* mUser[3] = {nullptr, nullptr, nullptr};
+    srtEvent* mHandler = nullptr;
+    gbDevice* mDevice = nullptr;
+};

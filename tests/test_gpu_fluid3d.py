@@ -262,3 +262,28 @@ def test_c2_full_size_one_step(cuda):
     r, rs = oracle_step(sc, sc.vel)
     errs = compare_fast(g, gs, r, rs, sc.pos)
     print("C2 1M fused-vs-restatement relative errors:", errs)
+
+
+def test_golden_fixture_bit_exact(cuda):
+    """The exact kernels reproduce the independent pure-Python restatement's fixture
+    (tests/golden/ref3d_hash_small.npz) bit for bit."""
+    from pathlib import Path
+    from libcl_gb300 import Fluid3DParams, default_params
+    from libcl_gb300.scenes import Scene3D
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ref3d_hash_small.npz")
+    p = default_params()
+    for (name, _), v in zip(Fluid3DParams._fields_[:13], g["params"]):
+        setattr(p, name, float(v))
+    sc = Scene3D("golden", g["pos0"].copy(), g["vel0"].copy(), p)
+    for fused in (False, True):
+        f = make_fluid(sc, fused=fused)
+        f.compute()
+        o, s = sorted_outputs(f, REF_BUCKETS), state(f)
+        for k in ("cell", "index", "spos", "svel"):
+            assert_bit_exact(o[k], g[k], k)
+        occ = g["occupied"]
+        assert np.array_equal(np.nonzero(o["cell_start"] != 0xFFFFFFFF)[0], occ)
+        assert_bit_exact(o["cell_start"][occ], g["cell_start"], "cellStart")
+        assert_bit_exact(o["cell_end"][occ], g["cell_end"], "cellEnd")
+        for k, gk in (("pos", "pos1"), ("vel", "vel1"), ("force", "force1")):
+            assert_bit_exact(s[k], g[gk], k)
