@@ -88,6 +88,17 @@ GBSPH_API int gbsph_radix_sort_cell_bounds(gbsph_radix_sort_t h, const uint32_t*
 GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream);
 GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h);
 
+/* Allocation-free sort (no counterpart in the reference): the same stable in-place sort as
+ * gbsph_radix_sort_compute for callers that cannot allocate device memory (a host framework
+ * that owns all device memory through its own allocator, real-time loops that must not stall
+ * on cudaMalloc/cudaFree, plugins with a fixed memory footprint). Its scratch is a static
+ * device array of about 4.5 MB that every GPU loading the library holds until exit.
+ * Limits: at most 262,144 pairs (GBSPH_ERR_TOO_LARGE beyond); the first call on a device
+ * looks up the array's address, so make it before any stream capture; all calls share the
+ * array, so calls that overlap on the GPU race; device-side timeouts are not reported. */
+GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t n_keys,
+                                       size_t n_values, int start_bit, int end_bit, void* stream);
+
 /* ------------------------------------------------------------------------------------------
  * 3D SPH fluid. Replaces `oclFluid3D` (libCL/phys/oclFluid3D.h:21-123,
  * libCL/phys/oclFluid3D.cpp:21-342).

@@ -67,6 +67,7 @@ SIGNATURES = {
     "gbsph_radix_sort_cell_bounds": (_I, [_P, _P, _SZ, _P, _P, _SZ, _P]),
     "gbsph_radix_sort_sync_status": (_I, [_P, _P]),
     "gbsph_radix_sort_last_error": (C.c_char_p, [_P]),
+    "gbsph_radix_sort_noalloc": (_I, [_P, _P, _SZ, _SZ, _I, _I, _P]),
     "gbsph_fluid3d_create": (_I, [C.POINTER(_P)]),
     "gbsph_fluid3d_destroy": (_I, [_P]),
     "gbsph_fluid3d_compile": (_I, [_P]),

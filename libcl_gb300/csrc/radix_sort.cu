@@ -17,6 +17,7 @@
 // The last pass can gather float4 payloads by the sorted value (the fluid's reorder stage).
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "device.cuh"
@@ -462,6 +463,112 @@ GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream) {
 
 GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h) {
     return h ? h->last_error.c_str() : "null handle";
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free variant of gbsph_radix_sort_compute.
+//
+// Some callers cannot call cudaMalloc: code that runs while a host framework owns all device
+// memory through its own fixed-budget allocator, real-time loops where cudaMalloc/cudaFree
+// would stall on an implicit device synchronisation, and plugins that must not change the
+// device's memory footprint after start-up. gbsph_radix_sort_noalloc serves them: its
+// scratch (histograms, tile counters, look-back words and the two ping-pong key/value pairs)
+// lives in the file-scope device array below, which every GPU that loads this library holds
+// until the process exits. The array's host-side name is only a stand-in for the symbol, so
+// its device address is looked up per device with cudaGetSymbolAddress.
+// ------------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_KEYS = 262144;  // 2^18 pairs
+constexpr size_t NOALLOC_STATUS_BYTES = (size_t)SORT_MAX_PASSES * ((NOALLOC_MAX_KEYS + SORT_TILE - 1) / SORT_TILE) * SORT_RADIX * 4;
+constexpr size_t NOALLOC_ERR_OFFSET = SORT_HEADER_BYTES + NOALLOC_STATUS_BYTES;  // one uint32 (256 B slot)
+constexpr size_t NOALLOC_TMP_OFFSET = NOALLOC_ERR_OFFSET + 256;
+constexpr size_t NOALLOC_BYTES = NOALLOC_TMP_OFFSET + 4ull * NOALLOC_MAX_KEYS * sizeof(uint32_t);  // ~4.5 MB
+static_assert(SORT_HEADER_BYTES % 256 == 0 && NOALLOC_ERR_OFFSET % 256 == 0, "256-byte aligned regions");
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device.
+cudaError_t noalloc_scratch(int device, void** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[device] = p;
+    }
+    *out = g_noalloc_ptr[device];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Same contract as gbsph_radix_sort_compute (stable LSD sort of (key, value) pairs on key
+// bits [start_bit, end_bit), in place, on `stream`), but no device memory is allocated:
+// * n_keys may not exceed 262,144 (GBSPH_ERR_TOO_LARGE otherwise);
+// * the first call on a device looks up the scratch array's device address, so make that
+//   first call before any stream capture begins;
+// * every call on a device shares the one scratch array and the call clears it with
+//   cudaMemsetAsync on `stream`; calls that overlap on the GPU (different streams without
+//   ordering between them) race on it and must not be issued;
+// * a device-side look-back timeout leaves the output undefined and is not reported here.
+GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t n_keys, size_t n_values,
+                                       int start_bit, int end_bit, void* stream) {
+    if (n_keys != n_values) return fail(nullptr, GBSPH_ERR_SIZE_MISMATCH, "noalloc sort: key and value counts differ");
+    if (n_keys > NOALLOC_MAX_KEYS)
+        return fail(nullptr, GBSPH_ERR_TOO_LARGE,
+                    "noalloc sort: " + std::to_string(n_keys) + " pairs exceed its limit of " +
+                        std::to_string(NOALLOC_MAX_KEYS));
+    if (start_bit < 0 || end_bit > 32 || end_bit < start_bit || (end_bit - start_bit) % 4 != 0)
+        return fail(nullptr, GBSPH_ERR_BIT_RANGE, "noalloc sort: bit range must be a multiple of 4 within [0, 32]");
+    if (n_keys == 0 || start_bit == end_bit) return GBSPH_OK;
+    if (!keys || !values) return fail(nullptr, GBSPH_ERR_ARGUMENT, "noalloc sort: null key or value pointer");
+    int device = 0;
+    GBSPH_CUDA_TRY(nullptr, cudaGetDevice(&device));
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return fail(nullptr, GBSPH_ERR_ARGUMENT, "noalloc sort: device ordinal too large");
+    void* base = nullptr;
+    GBSPH_CUDA_TRY(nullptr, noalloc_scratch(device, &base));
+    char* b = (char*)base;
+    const uint32_t n = (uint32_t)n_keys;
+    const int P = sort_passes(start_bit, end_bit);
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* err = (uint32_t*)(b + NOALLOC_ERR_OFFSET);
+    uint32_t* tmp = (uint32_t*)(b + NOALLOC_TMP_OFFSET);
+    GBSPH_CUDA_TRY(nullptr, onesweep_prepare(b, n, P, s));  // histogram, counters, look-back words
+    GBSPH_CUDA_TRY(nullptr, cudaMemsetAsync(err, 0, 4, s));
+    GBSPH_CUDA_TRY(nullptr, onesweep_histogram(keys, n, start_bit, end_bit, b, s));
+    OnesweepArgs a;
+    a.keys_in = keys;
+    a.vals_in = values;
+    a.tmp_keys[0] = tmp;
+    a.tmp_vals[0] = tmp + NOALLOC_MAX_KEYS;
+    a.tmp_keys[1] = tmp + 2 * NOALLOC_MAX_KEYS;
+    a.tmp_vals[1] = tmp + 3 * NOALLOC_MAX_KEYS;
+    a.n = n;
+    a.start_bit = start_bit;
+    a.end_bit = end_bit;
+    a.scratch = b;
+    a.err = err;
+    if (P == 1) {
+        a.keys_out = a.tmp_keys[0];
+        a.vals_out = a.tmp_vals[0];
+        GBSPH_CUDA_TRY(nullptr, onesweep_passes(a, s));
+        GBSPH_CUDA_TRY(nullptr, cudaMemcpyAsync(keys, a.keys_out, n * 4ull, cudaMemcpyDeviceToDevice, s));
+        GBSPH_CUDA_TRY(nullptr, cudaMemcpyAsync(values, a.vals_out, n * 4ull, cudaMemcpyDeviceToDevice, s));
+    } else {
+        a.keys_out = keys;
+        a.vals_out = values;
+        GBSPH_CUDA_TRY(nullptr, onesweep_passes(a, s));
+    }
+    return GBSPH_OK;
 }
 
 }  // extern "C"
