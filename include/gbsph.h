@@ -240,6 +240,88 @@ GBSPH_API int gbsph_fluid3d_sync_status(gbsph_fluid3d_t h, void* stream);
 GBSPH_API int gbsph_fluid3d_stage_times(gbsph_fluid3d_t h, float* ms, int max_stages);
 GBSPH_API const char* gbsph_fluid3d_last_error(gbsph_fluid3d_t h);
 
+/* ------------------------------------------------------------------------------------------
+ * 2D SPH fluid: the reference's double-density relaxation model with an image-sampled wall
+ * field. Replaces `oclFluid2D` (libCL/phys/oclFluid2D.h:22-138, libCL/phys/oclFluid2D.cpp:18-362,
+ * libCL/phys/oclFluid2D.cl:14-443). The step is clAdvanceState -> clHash -> sort bits [0,24) ->
+ * clReorder -> clInitBounds -> clFindBounds -> clComputePressure -> clComputePosition ->
+ * clUpdateState (libCL/phys/oclFluid2D.cpp:256-362). The wall field is two W x H RGBA images
+ * stored with half-float precision (libCL/phys/oclFluid2D.cpp:72-75), sampled bilinearly with
+ * normalised, clamp-to-edge coordinates; here they are float4 arrays whose values are rounded
+ * to half precision when written. As in the reference, no integrate hook is called.
+ * ---------------------------------------------------------------------------------------- */
+
+/* oclFluid2D::Params (libCL/phys/oclFluid2D.h:42-60), field for field. */
+typedef struct gbsph_fluid2d_params {
+    float dT;
+    float h;
+    float containerW;
+    float containerH;
+    float cellSize;
+    int32_t cellCountX;
+    int32_t cellCountY;
+    float particleSize;
+    float particleMass;
+    float p0; /* restDensity in the kernels' System struct */
+    float vmax;
+    float B;
+} gbsph_fluid2d_params;
+
+/* oclFluid2D::Particle (libCL/phys/oclFluid2D.h:62-69): 24 bytes. */
+typedef struct gbsph_particle2d {
+    float pos[2];
+    float vel[2];
+    float mass;
+    float unused;
+} gbsph_particle2d;
+
+enum {
+    GBSPH2D_BUF_STATE = 0,         /* gbsph_particle2d[N], particle order (settable) */
+    GBSPH2D_BUF_SORTED_STATE = 1,  /* gbsph_particle2d[N], cell order */
+    GBSPH2D_BUF_INDEX = 2,         /* uint32[N] sorted slot -> particle */
+    GBSPH2D_BUF_CELL = 3,          /* uint32[N] sorted keys */
+    GBSPH2D_BUF_PRESSURE = 4,      /* float4[N] (density, near density, pressure, near pressure), cell order */
+    GBSPH2D_BUF_RELAXED = 5,       /* float2[N] relaxed positions, cell order */
+    GBSPH2D_BUF_PREVIOUS = 6,      /* float2[N] positions before the step, particle order */
+    GBSPH2D_BUF_BORDER_STATE = 7,  /* float4[W*H] wall (density, near density, pressure, near pressure) */
+    GBSPH2D_BUF_BORDER_VECTOR = 8  /* float4[W*H] wall (normal x, normal y, distance, 0) */
+};
+
+typedef struct gbsph_fluid2d_s* gbsph_fluid2d_t;
+
+/* oclFluid2D(oclContext&, oclProgram*) -- libCL/phys/oclFluid2D.cpp:18-85: 128*128 particles,
+ * zeroed state, 256x256 zeroed wall images. */
+GBSPH_API int gbsph_fluid2d_create(gbsph_fluid2d_t* out);
+GBSPH_API int gbsph_fluid2d_destroy(gbsph_fluid2d_t h);
+/* compile() -- libCL/phys/oclFluid2D.cpp:230-248: clInitFluid's defaults
+ * (libCL/phys/oclFluid2D.cl:136-151) and a cell table of
+ * (cellCountX*cellCountY/256 + 1)*256 entries. */
+GBSPH_API int gbsph_fluid2d_compile(gbsph_fluid2d_t h);
+/* Fills `p` with clInitFluid's defaults (host only). */
+GBSPH_API int gbsph_fluid2d_default_params(gbsph_fluid2d_params* p);
+/* setParticleCount -- libCL/phys/oclFluid2D.cpp:92-112. */
+GBSPH_API int gbsph_fluid2d_set_particle_count(gbsph_fluid2d_t h, size_t n);
+GBSPH_API size_t gbsph_fluid2d_get_particle_count(gbsph_fluid2d_t h);
+/* setStateBuffer -- libCL/phys/oclFluid2D.cpp:119-129: borrowed gbsph_particle2d[count],
+ * count must equal the particle count. */
+GBSPH_API int gbsph_fluid2d_set_state_buffer(gbsph_fluid2d_t h, void* device_ptr, size_t count);
+/* getStateBuffer and the internal buffers (GBSPH2D_BUF_*). */
+GBSPH_API void* gbsph_fluid2d_get_buffer(gbsph_fluid2d_t h, int which, size_t* count);
+/* getParameters -- libCL/phys/oclFluid2D.cpp:163-166. Read at every compute(). */
+GBSPH_API gbsph_fluid2d_params* gbsph_fluid2d_get_params(gbsph_fluid2d_t h);
+/* computeBorder(oclImage2D*) -- libCL/phys/oclFluid2D.cpp:131-146, clComputeBorder
+ * (libCL/phys/oclFluid2D.cl:358-443): `mask` is a device float4[width*height] RGBA image whose
+ * .w == 1.0 marks wall pixels; the wall images are resized to width x height. */
+GBSPH_API int gbsph_fluid2d_compute_border(gbsph_fluid2d_t h, const float* mask, int width, int height,
+                                           void* stream);
+/* compute(oclDevice&) -- libCL/phys/oclFluid2D.cpp:256-362. */
+GBSPH_API int gbsph_fluid2d_compute(gbsph_fluid2d_t h, void* stream);
+/* The cell table as two uint32 arrays of n_cells (= the compiled table size) entries. */
+GBSPH_API int gbsph_fluid2d_get_cell_bounds(gbsph_fluid2d_t h, uint32_t* cell_start, uint32_t* cell_end,
+                                            size_t n_cells, void* stream);
+GBSPH_API int gbsph_fluid2d_sync_status(gbsph_fluid2d_t h, void* stream);
+GBSPH_API const char* gbsph_fluid2d_last_error(gbsph_fluid2d_t h);
+
 #ifdef __cplusplus
 }
 #endif

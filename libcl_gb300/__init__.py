@@ -52,6 +52,17 @@ class Fluid3DParams(C.Structure):
         ("dims", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
+class Fluid2DParams(C.Structure):
+    """gbsph_fluid2d_params: oclFluid2D::Params (libCL/phys/oclFluid2D.h:42-60)."""
+    _fields_ = [("dT", C.c_float), ("h", C.c_float), ("containerW", C.c_float), ("containerH", C.c_float),
+                ("cellSize", C.c_float), ("cellCountX", C.c_int32), ("cellCountY", C.c_int32),
+                ("particleSize", C.c_float), ("particleMass", C.c_float), ("p0", C.c_float), ("vmax", C.c_float),
+                ("B", C.c_float)]
+
+
+(BUF2D_STATE, BUF2D_SORTED_STATE, BUF2D_INDEX, BUF2D_CELL, BUF2D_PRESSURE, BUF2D_RELAXED, BUF2D_PREVIOUS,
+ BUF2D_BORDER_STATE, BUF2D_BORDER_VECTOR) = range(9)
+
 HOOK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 LOG_FN = C.CFUNCTYPE(None, C.c_int, C.c_char_p, C.c_void_p)
 
@@ -86,6 +97,20 @@ SIGNATURES = {
     "gbsph_fluid3d_sync_status": (_I, [_P, _P]),
     "gbsph_fluid3d_last_error": (C.c_char_p, [_P]),
     "gbsph_fluid3d_stage_times": (_I, [_P, C.POINTER(C.c_float), _I]),
+    "gbsph_fluid2d_create": (_I, [C.POINTER(_P)]),
+    "gbsph_fluid2d_destroy": (_I, [_P]),
+    "gbsph_fluid2d_compile": (_I, [_P]),
+    "gbsph_fluid2d_default_params": (_I, [C.POINTER(Fluid2DParams)]),
+    "gbsph_fluid2d_set_particle_count": (_I, [_P, _SZ]),
+    "gbsph_fluid2d_get_particle_count": (_SZ, [_P]),
+    "gbsph_fluid2d_set_state_buffer": (_I, [_P, _P, _SZ]),
+    "gbsph_fluid2d_get_buffer": (_P, [_P, _I, C.POINTER(_SZ)]),
+    "gbsph_fluid2d_get_params": (C.POINTER(Fluid2DParams), [_P]),
+    "gbsph_fluid2d_compute_border": (_I, [_P, _P, _I, _I, _P]),
+    "gbsph_fluid2d_compute": (_I, [_P, _P]),
+    "gbsph_fluid2d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
+    "gbsph_fluid2d_sync_status": (_I, [_P, _P]),
+    "gbsph_fluid2d_last_error": (C.c_char_p, [_P]),
 }
 
 _lib = None
@@ -314,6 +339,91 @@ class Fluid3D:
         if n < 0:
             raise GbsphError(n, self.last_error())
         return {STAGE_TIME_NAMES[i]: float(buf[i]) for i in range(n)}
+
+
+class Fluid2D:
+    """oclFluid2D (libCL/phys/oclFluid2D.h:22-138): the reference's 2D double-density
+    relaxation model. State is gbsph_particle2d (pos.xy, vel.xy, mass, unused) per particle."""
+
+    cLocalSize = 256
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_fluid2d_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_fluid2d_create")
+        self._h = h
+        self._borrowed = None
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_fluid2d_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_fluid2d_last_error(self._h).decode())
+
+    def compile(self) -> None:
+        self._check(self._lib.gbsph_fluid2d_compile(self._h))
+
+    def compute(self, stream=None) -> None:
+        self._check(self._lib.gbsph_fluid2d_compute(self._h, _stream(stream)))
+
+    def setParticleCount(self, n: int) -> None:
+        self._check(self._lib.gbsph_fluid2d_set_particle_count(self._h, n))
+
+    def getParticleCount(self) -> int:
+        return int(self._lib.gbsph_fluid2d_get_particle_count(self._h))
+
+    def getParameters(self) -> Fluid2DParams:
+        return self._lib.gbsph_fluid2d_get_params(self._h).contents
+
+    def setStateBuffer(self, t) -> None:
+        self._check(self._lib.gbsph_fluid2d_set_state_buffer(self._h, _ptr(t), t.numel() // 6))
+        self._borrowed = t
+
+    def computeBorder(self, mask, stream=None) -> None:
+        """mask: CUDA float32 tensor [H, W, 4]; .w == 1 marks wall pixels."""
+        h, w = mask.shape[0], mask.shape[1]
+        self._check(self._lib.gbsph_fluid2d_compute_border(self._h, _ptr(mask), w, h, _stream(stream)))
+
+    def buffer(self, which: int):
+        import torch
+        count = C.c_size_t()
+        p = self._lib.gbsph_fluid2d_get_buffer(self._h, which, C.byref(count))
+        if not p:
+            raise GbsphError(ERR_ARGUMENT, f"no buffer {which}")
+        if which == BUF2D_STATE and self._borrowed is not None:
+            return self._borrowed
+        n = count.value
+        cols = {BUF2D_STATE: 6, BUF2D_SORTED_STATE: 6, BUF2D_PRESSURE: 4, BUF2D_RELAXED: 2, BUF2D_PREVIOUS: 2,
+                BUF2D_BORDER_STATE: 4, BUF2D_BORDER_VECTOR: 4}.get(which)
+        if cols is None:
+            return _device_view(p, n, torch.int32, (n,))
+        return _device_view(p, n * cols, torch.float32, (n, cols))
+
+    def getStateBuffer(self):
+        return self.buffer(BUF2D_STATE)
+
+    def cell_bounds(self, n_cells: int, stream=None):
+        import torch
+        cs = torch.empty(n_cells, dtype=torch.int32, device="cuda")
+        ce = torch.empty(n_cells, dtype=torch.int32, device="cuda")
+        self._check(self._lib.gbsph_fluid2d_get_cell_bounds(self._h, _ptr(cs), _ptr(ce), n_cells, _stream(stream)))
+        return cs, ce
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_fluid2d_sync_status(self._h, _stream(stream))
+
+
+def default_params_2d() -> Fluid2DParams:
+    p = Fluid2DParams()
+    rc = load_library().gbsph_fluid2d_default_params(C.byref(p))
+    if rc:
+        raise GbsphError(rc, "default_params_2d")
+    return p
 
 
 def params_derive(p: Fluid3DParams) -> None:

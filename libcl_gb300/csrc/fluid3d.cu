@@ -17,7 +17,9 @@ using namespace gbsph;
 
 namespace {
 
-constexpr uint32_t BRICK_CAP = 2048;  // staged candidates per brick (float4 per array)
+constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * CELL_LIST_MAX * 2 +
+                                (size_t)BRICK_WARPS * 32 * WLIST_STRIDE * 2;
+constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
 
 struct DevBuf {
     void* ptr = nullptr;
@@ -64,6 +66,8 @@ struct gbsph_fluid3d_s {
     float4* svel = nullptr;
     uint32_t *keys_a = nullptr, *keys_b = nullptr, *keys_c = nullptr;
     uint32_t *vals_a = nullptr, *vals_b = nullptr, *index = nullptr, *bricks = nullptr;
+    uint16_t* nbr = nullptr;      // per particle NBR_CAP neighbour slots (density -> forces)
+    uint8_t* nbr_flag = nullptr;  // per particle: 1 = scan instead of the list
     uint32_t* hash_tables = nullptr;  // cell start / end, REF_BUCKETS each
     uint2* table = nullptr;           // LINEAR_GRID interleaved table
     size_t table_cells = 0;
@@ -73,7 +77,7 @@ struct gbsph_fluid3d_s {
     uint32_t* err = nullptr;
     gbsph_fluid3d_hook_fn hook = nullptr;
     void* hook_user = nullptr;
-    int opt_fused = 1, opt_graph = 1, opt_bw = 8, opt_profile = 0;
+    int opt_fused = 1, opt_graph = 1, opt_bw = 16, opt_profile = 0;
     cudaEvent_t ev[6] = {};
     bool ev_valid = false;
     int dens_blocks = 0, force_blocks = 0;
@@ -197,7 +201,7 @@ void free_particle_arrays(H* h) {
 int alloc_particle_arrays(H* h, size_t n) {
     free_particle_arrays(h);
     const size_t n4 = (n + 63) & ~size_t(63);
-    const size_t bytes = n4 * (2 * 16 + 7 * 4);
+    const size_t bytes = n4 * (2 * 16 + 7 * 4 + NBR_CAP * 2 + 1);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->pblock, bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->pblock, 0, bytes));
     char* p = (char*)h->pblock;
@@ -210,6 +214,9 @@ int alloc_particle_arrays(H* h, size_t n) {
         *a = (uint32_t*)p;
         p += n4 * 4;
     }
+    h->nbr = (uint16_t*)p;
+    p += n4 * NBR_CAP * 2;
+    h->nbr_flag = (uint8_t*)p;
     h->scratch_bytes = onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, h->scratch_bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->scratch, 0, h->scratch_bytes));
@@ -335,20 +342,21 @@ int st_forces_exact(H* h, const KParams& kp, cudaStream_t s) {
 }
 
 int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
-    const size_t smem = (size_t)BRICK_CAP * 16;
-    if (kp.dims == 2)
-        k_density_brick<2><<<h->dens_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
-    else
-        k_density_brick<3><<<h->dens_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
+    auto launch = [&](auto kern) {
+        kern<<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp,
+                                                                 h->nbr, h->nbr_flag, h->err);
+    };
+    if (kp.dims == 2) launch(k_density_brick<2>);
+    else launch(k_density_brick<3>);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
 
 int st_force_brick(H* h, const KParams& kp, cudaStream_t s, bool fused) {
-    const size_t smem = (size_t)BRICK_CAP * 32;
     auto launch = [&](auto kern) {
-        kern<<<h->force_blocks, BRICK_THREADS, smem, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2),
-                                                          h->table, h->bricks, counters(h), kp, BRICK_CAP, h->err);
+        kern<<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2),
+                                                                h->table, h->bricks, counters(h), kp, h->nbr,
+                                                                h->nbr_flag, h->err);
     };
     if (kp.dims == 2) {
         if (fused) launch(k_force_brick<2, true>);
@@ -455,7 +463,7 @@ std::vector<char> graph_key(const H* h, const KParams& kp) {
         std::memcpy(p, &h->buf[i].ptr, sizeof(void*));
         p += sizeof(void*);
     }
-    int o[4] = {h->opt_fused, h->opt_bw, (int)h->table_cells, h->dens_blocks};
+    int o[4] = {h->opt_fused, h->opt_bw, (int)h->table_cells, 0};
     std::memcpy(p, o, sizeof(o));
     return k;
 }
@@ -463,16 +471,16 @@ std::vector<char> graph_key(const H* h, const KParams& kp) {
 int setup_kernels(H* h) {
     const int sms = num_sms();
     int nb = 0;
-    const size_t dsm = (size_t)BRICK_CAP * 16, fsm = (size_t)BRICK_CAP * 32;
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_brick<3>, BRICK_THREADS, dsm));
+    const int dsm = (int)DENSITY_SMEM, fsm = (int)FORCE_SMEM;
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_brick<3>, BRICK_THREADS, DENSITY_SMEM));
     h->dens_blocks = std::max(1, nb) * sms;
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true>, BRICK_THREADS, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true>, BRICK_THREADS, FORCE_SMEM));
     h->force_blocks = std::max(1, nb) * sms;
     return GBSPH_OK;
 }

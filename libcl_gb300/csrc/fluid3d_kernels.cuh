@@ -483,21 +483,47 @@ __device__ __forceinline__ float reduce_q(float v, uint32_t q, uint32_t Q, uint3
     return v;
 }
 
+// Staged candidates per brick. The density and force kernels use the same value so that they
+// stage (or fall back for) exactly the same bricks: the neighbour lists the density kernel
+// records are indices into that staging.
+constexpr uint32_t BRICK_CAP = 1536;
+constexpr uint32_t CELL_LIST_MAX = 512;  // candidates of one target cell, per warp (uint16)
+constexpr uint32_t NBR_CAP = 64;         // neighbour slots per particle (uint16), split over the Q lanes
+constexpr uint16_t NBR_END = 0xFFFFu;    // terminates a lane's neighbour sub-list
+constexpr uint32_t WLIST_STRIDE = NBR_CAP + 2;  // shared-memory stride per target (33 words: no bank conflicts)
+constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists the force kernel stages
+
+// Slots of each lane's sub-list when Q lanes share a target: a multiple of 8 (one 16-byte
+// vector) when Q <= 8, else 4 or 2, so sub-lists start on their load width.
+__device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
+    const uint32_t s = NBR_CAP / Q;
+    return s >= 8 ? (s & ~7u) : (s >= 4 ? 4u : 2u);
+}
+
 // Density + pressure for every particle of the occupied bricks (persistent CTAs).
 // Writes sorted position .w = density and sorted velocity .w = pressure, as
-// clCalculateDensity does (libCL/phys/oclFluid3D.cl:189-199).
+// clCalculateDensity does (libCL/phys/oclFluid3D.cl:189-199). Per target cell, a warp first
+// lists the cell's candidates (the 3 cells of each neighbour row, in row order) as staged
+// indices, then lanes (target, stride q) walk that list. Every target also meets itself
+// (r^2 = 0, term h^6, count 1); that term is removed after the sum instead of testing the
+// index of every candidate. Each lane records its in-range neighbours (r^2 > 0) as staged
+// indices in its own sub-list of nbr[gi][NBR_CAP] (in candidate order, NBR_END-terminated);
+// nbr_flag[gi] = 1 when a sub-list overflowed or the brick could not be staged.
 template <int DIMS>
 __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
                                                                  float4* __restrict__ svel,
                                                                  const uint2* __restrict__ table,
                                                                  const uint32_t* __restrict__ bricks,
                                                                  uint32_t* counters, KParams kp,
-                                                                 uint32_t cap, uint32_t* err) {
+                                                                 uint16_t* __restrict__ nbr,
+                                                                 uint8_t* __restrict__ nbr_flag, uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;  // the brick's own row
-    extern __shared__ float4 s_buf[];
+    extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, per-warp candidate lists, per-warp neighbour lists
     __shared__ BrickShared S;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint16_t* clist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * CELL_LIST_MAX;
+    uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + BRICK_WARPS * CELL_LIST_MAX + warp * 32 * WLIST_STRIDE;
     if (t == 0) {
         mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
         fence_mbar_init();
@@ -505,6 +531,8 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t n_bricks = counters[0];
+    const float h2 = kp.h2, thr = kp.r2_thresh;
+    const uint32_t lt = lanemask_lt();
     for (;;) {
         if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
         __syncthreads();
@@ -512,10 +540,21 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
         if (b >= n_bricks) break;
         int x0, ncell;
         brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
-        const bool staged = brick_stage<DIMS, 1>(S, s_buf, cap, spos, nullptr);
+        const bool staged = brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr);
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
+            uint32_t T = 0;
+            if (staged) {
+                for (int r = 0; r < R; ++r) {
+                    const uint32_t s0 = S.base[r] + S.off[r][c], len = S.off[r][c + 3] - S.off[r][c];
+                    if (T + len <= CELL_LIST_MAX)
+                        for (uint32_t k = lane; k < len; k += 32) clist[T + k] = (uint16_t)(s0 + k);
+                    T += len;
+                }
+                __syncwarp();
+            }
+            const bool flat = staged && T <= CELL_LIST_MAX;
             for (uint32_t g0 = 0; g0 < nt; g0 += 32) {
                 const uint32_t tg = min(32u, nt - g0), Q = 32u / tg;
                 const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
@@ -523,48 +562,115 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                 const uint32_t tl = t0 + g0 + ti;
                 const uint32_t gi = S.lo[RC] + tl;
                 const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
-                float acc = 0.0f, cntf = 0.0f;
+                const uint32_t sub = nbr_sub(Q);
+                uint16_t* my = wlist + ti * WLIST_STRIDE + q * sub;
+                float acc = 0.0f, cnt = 0.0f;
+                bool ovf = !flat;
                 if (active) {
-#pragma unroll 1
-                    for (int r = 0; r < R; ++r) {
-                        const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
-                        const uint32_t rlo = S.lo[r], hi = S.off[r][c + 3];
+                    if (flat) {
+                        uint32_t nk = 0;
 #pragma unroll 4
-                        for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
-                            const float4 pj = rp[j];
+                        for (uint32_t k = q; k < T; k += Q) {
+                            const uint32_t idx = clist[k];
+                            const float4 pj = s_buf[idx];
                             const float dx = pi.x - pj.x, dy = pi.y - pj.y;
                             float r2 = fmaf(dy, dy, dx * dx);
                             if (DIMS == 3) {
                                 const float dz = pi.z - pj.z;
                                 r2 = fmaf(dz, dz, r2);
                             }
-                            if (r2 < kp.r2_thresh && rlo + j != gi) {
-                                const float tt = kp.h2 - r2;
+                            const bool in = r2 < thr;
+                            const float tt = in ? h2 - r2 : 0.0f;
+                            acc = fmaf(tt * tt, tt, acc);
+                            cnt += in ? 1.0f : 0.0f;
+                            // branch-free append: the slot after the last real entry is
+                            // overwritten by the terminator below
+                            my[min(nk, sub - 1)] = (uint16_t)idx;
+                            nk += (in && r2 > 0.0f) ? 1u : 0u;
+                        }
+                        if (nk < sub) my[nk] = NBR_END;
+                        ovf = nk > sub;
+                    } else {
+#pragma unroll 1
+                        for (int r = 0; r < R; ++r) {
+                            const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
+                            const uint32_t hi = S.off[r][c + 3];
+                            for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
+                                const float4 pj = rp[j];
+                                const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                                float r2 = fmaf(dy, dy, dx * dx);
+                                if (DIMS == 3) {
+                                    const float dz = pi.z - pj.z;
+                                    r2 = fmaf(dz, dz, r2);
+                                }
+                                const bool in = r2 < thr;
+                                const float tt = in ? h2 - r2 : 0.0f;
                                 acc = fmaf(tt * tt, tt, acc);
-                                cntf += 1.0f;
+                                cnt += in ? 1.0f : 0.0f;
                             }
                         }
                     }
                 }
                 acc = reduce_q(acc, q, Q, tg);
-                cntf = reduce_q(cntf, q, Q, tg);
+                cnt = reduce_q(cnt, q, Q, tg);
+                uint32_t gm = 0;  // lanes sharing this lane's target
+                for (uint32_t k = 0; k < Q; ++k) gm |= 1u << (ti + k * tg);
+                const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & gm;
+                (void)lt;
                 if (active && q == 0) {
+                    acc -= h2 * h2 * h2;  // the target's own term
+                    cnt -= 1.0f;
                     float rho = kp.rho0, p = kp.p0;
-                    if (cntf > 2.5f) {
+                    if (cnt > 2.5f) {
                         rho = fmaxf(1.0f, kp.mass * kp.kconst * acc);
                         p = kp.p0 + kp.stiff * (rho - kp.rho0);
                     }
                     spos[gi] = make_float4(pi.x, pi.y, pi.z, rho);
                     reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
+                    nbr_flag[gi] = om ? 1 : 0;
                 }
+                // copy the group's lists (tg consecutive particles) out with 16-byte stores
+                __syncwarp();
+                if (flat) {
+                    const uint32_t* src = reinterpret_cast<const uint32_t*>(wlist);
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(nbr + (size_t)(S.lo[RC] + t0 + g0) * NBR_CAP);
+                    for (uint32_t tt = 0; tt < tg; ++tt)  // NBR_CAP / 2 = 32 words per target
+                        dst[tt * (NBR_CAP / 2) + lane] = src[tt * (WLIST_STRIDE / 2) + lane];
+                }
+                __syncwarp();
             }
+            __syncwarp();  // clist is rebuilt for the warp's next cell
         }
     }
 }
 
-// Forces (pressure + viscosity) for every particle of the occupied bricks. With FUSED the
-// clip-box, integrate-force, gravity and integrate-velocity stages follow in registers;
-// otherwise the SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
+// Pressure + viscosity contribution of one in-range neighbour (acc: pressure xyz, viscosity xyz).
+template <int DIMS>
+__device__ __forceinline__ void force_pair(const float4& pi, const float4& vi, float inv_rho_i, const float4& pj,
+                                           const float4& vj, float h, float* acc) {
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = DIMS == 3 ? pi.z - pj.z : 0.0f;
+    float r2 = fmaf(dy, dy, dx * dx);
+    if (DIMS == 3) r2 = fmaf(dz, dz, r2);
+    const float inv = rsqrtf(r2);
+    const float vlen = r2 * inv;
+    const float hr = h - vlen;
+    const float dd = inv_rho_i * __frcp_rn(pj.w);  // 1 / (rho_i rho_j)
+    const float sp = (vi.w + vj.w) * dd * hr * hr * inv;
+    acc[0] = fmaf(sp, dx, acc[0]);
+    acc[1] = fmaf(sp, dy, acc[1]);
+    acc[2] = fmaf(sp, dz, acc[2]);
+    const float cv = hr * dd;
+    acc[3] = fmaf(vj.x - vi.x, cv, acc[3]);
+    acc[4] = fmaf(vj.y - vi.y, cv, acc[4]);
+    acc[5] = fmaf(vj.z - vi.z, cv, acc[5]);
+}
+
+// Forces (pressure + viscosity) for every particle of the occupied bricks. The brick's rows
+// are staged exactly as in k_density_brick, and each lane evaluates only the in-range pairs
+// that the density kernel recorded in its sub-list. Targets whose lists are unusable
+// (overflow, unstaged brick) are handled by scanning the rows. With FUSED the clip-box,
+// integrate-force, gravity and integrate-velocity stages follow in registers; otherwise the
+// SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
 template <int DIMS, bool FUSED>
 __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __restrict__ spos,
                                                                const float4* __restrict__ svel,
@@ -575,10 +681,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                                                                const uint2* __restrict__ table,
                                                                const uint32_t* __restrict__ bricks,
                                                                uint32_t* counters, KParams kp,
-                                                               uint32_t cap, uint32_t* err) {
+                                                               const uint16_t* __restrict__ nbr,
+                                                               const uint8_t* __restrict__ nbr_flag,
+                                                               uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;
-    extern __shared__ float4 s_buf[];  // [cap] positions, then [cap] velocities
+    // [BRICK_CAP] positions, [BRICK_CAP] velocities, then the neighbour lists of up to
+    // LIST_STAGE_MAX targets
+    extern __shared__ float4 s_buf[];
     __shared__ BrickShared S;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     if (t == 0) {
@@ -588,6 +698,9 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
     __syncthreads();
     uint32_t phase = 0;
     const uint32_t n_bricks = counters[0];
+    const float4* s_pos = s_buf;
+    const float4* s_vel = s_buf + BRICK_CAP;
+    uint16_t* s_lists = reinterpret_cast<uint16_t*>(s_buf + 2 * BRICK_CAP);
     for (;;) {
         if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
         __syncthreads();
@@ -595,7 +708,31 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
         if (b >= n_bricks) break;
         int x0, ncell;
         brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
-        const bool staged = brick_stage<DIMS, 2>(S, s_buf, cap, spos, svel);
+        // the brick's targets are consecutive particles: stage their lists with the rows
+        const uint32_t tfirst = S.lo[RC] + S.off[RC][1];
+        const uint32_t ntarg = S.off[RC][ncell + 1] - S.off[RC][1];
+        const bool lists_staged = ntarg <= LIST_STAGE_MAX && S.rcnt[RC] > 0;
+        if (t == 0) {
+            uint32_t acc = 0;
+            for (int r = 0; r < R; ++r) {
+                S.base[r] = acc;
+                acc += S.rcnt[r];
+            }
+            S.total = acc;
+            if (acc <= BRICK_CAP && acc > 0) {
+                const uint32_t lbytes = lists_staged ? ntarg * NBR_CAP * 2 : 0u;
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 32u + lbytes);
+                for (int r = 0; r < R; ++r) {
+                    if (!S.rcnt[r]) continue;
+                    bulk_g2s(s_buf + S.base[r], spos + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                    bulk_g2s(s_buf + BRICK_CAP + S.base[r], svel + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                }
+                if (lbytes) bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, reinterpret_cast<uint64_t*>(&S.bar));
+            }
+        }
+        __syncthreads();
+        const bool staged = S.total <= BRICK_CAP && S.total > 0;
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
@@ -605,60 +742,81 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                 const bool active = q < Q;
                 const uint32_t tl = t0 + g0 + ti;
                 const uint32_t gi = S.lo[RC] + tl;
-                const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
-                const float4 vi = staged ? s_buf[cap + S.base[RC] + tl] : svel[gi];
+                const float4 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
+                const float4 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
                 const float inv_rho_i = 1.0f / pi.w;
-                float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-                if (active) {
+                float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+                // prefetch what the integration needs so its latency overlaps the pair loop
+                uint32_t o = 0;
+                float4 f_o = make_float4(0.f, 0.f, 0.f, 0.f), v_o = f_o, p_o = f_o;
+                if (active && q == 0) {
+                    o = index[gi];
+                    f_o = force[o];
+                    if (FUSED) {
+                        v_o = vel[o];
+                        p_o = pos[o];
+                    }
+                }
+                const bool scan = !staged || nbr_flag[gi] != 0;
+                if (active && !scan) {
+                    const uint32_t sub = nbr_sub(Q);
+                    const uint16_t* my = (lists_staged ? s_lists + (size_t)(gi - tfirst) * NBR_CAP
+                                                       : nbr + (size_t)gi * NBR_CAP) + q * sub;
+                    bool done = false;
+                    for (uint32_t k0 = 0; k0 < sub && !done; k0 += 8) {
+                        uint32_t w[4];  // up to 8 entries, two per word
+                        if (sub >= 8) {
+                            const uint4 v = *reinterpret_cast<const uint4*>(my + k0);
+                            w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+                        } else if (sub == 4) {
+                            const uint2 v = *reinterpret_cast<const uint2*>(my);
+                            w[0] = v.x; w[1] = v.y; w[2] = w[3] = 0xFFFFFFFFu;
+                        } else {
+                            w[0] = *reinterpret_cast<const uint32_t*>(my);
+                            w[1] = w[2] = w[3] = 0xFFFFFFFFu;
+                        }
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) {
+                            const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                            if (idx == NBR_END) {
+                                done = true;
+                                break;
+                            }
+                            force_pair<DIMS>(pi, vi, inv_rho_i, s_pos[idx], s_vel[idx], kp.h, acc);
+                        }
+                    }
+                } else if (active) {
 #pragma unroll 1
                     for (int r = 0; r < R; ++r) {
-                        const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
-                        const float4* rv = staged ? s_buf + cap + S.base[r] : svel + S.lo[r];
-                        const uint32_t rlo = S.lo[r], hi = S.off[r][c + 3];
-#pragma unroll 2
+                        const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
+                        const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
+                        const uint32_t hi = S.off[r][c + 3];
                         for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
                             const float4 pj = rp[j];
                             const float dx = pi.x - pj.x, dy = pi.y - pj.y;
-                            const float dz = DIMS == 3 ? pi.z - pj.z : 0.0f;
                             float r2 = fmaf(dy, dy, dx * dx);
-                            if (DIMS == 3) r2 = fmaf(dz, dz, r2);
-                            if (r2 < kp.r2_thresh && rlo + j != gi) {
-                                const float4 vj = rv[j];
-                                const float inv = rsqrtf(r2);
-                                const float vlen = r2 * inv;
-                                const float hr = kp.h - vlen;
-                                const float dd = inv_rho_i * __frcp_rn(pj.w);  // 1/(rho_i rho_j)
-                                const float sp = (vi.w + vj.w) * dd * hr * hr * inv;
-                                px = fmaf(sp, dx, px);
-                                py = fmaf(sp, dy, py);
-                                pz = fmaf(sp, dz, pz);
-                                const float cvv = hr * dd;
-                                qx = fmaf(vj.x - vi.x, cvv, qx);
-                                qy = fmaf(vj.y - vi.y, cvv, qy);
-                                qz = fmaf(vj.z - vi.z, cvv, qz);
+                            if (DIMS == 3) {
+                                const float dz = pi.z - pj.z;
+                                r2 = fmaf(dz, dz, r2);
                             }
+                            if (r2 < kp.r2_thresh && r2 > 0.0f) force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
                         }
                     }
                 }
-                px = reduce_q(px, q, Q, tg);
-                py = reduce_q(py, q, Q, tg);
-                pz = reduce_q(pz, q, Q, tg);
-                qx = reduce_q(qx, q, Q, tg);
-                qy = reduce_q(qy, q, Q, tg);
-                qz = reduce_q(qz, q, Q, tg);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) acc[k] = reduce_q(acc[k], q, Q, tg);
                 if (active && q == 0) {
-                    const uint32_t o = index[gi];
-                    float4 f = force[o];
-                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, px), __fmul_rn(kp.cvisc, qx)), kp.mass));
-                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, py), __fmul_rn(kp.cvisc, qy)), kp.mass));
-                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, pz), __fmul_rn(kp.cvisc, qz)), kp.mass));
+                    float4 f = f_o;
+                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(kp.cvisc, acc[3])), kp.mass));
+                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(kp.cvisc, acc[4])), kp.mass));
+                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(kp.cvisc, acc[5])), kp.mass));
                     f.w = 0.0f;
                     if (FUSED) {
                         f = clip_box_force(kp, pi, vi, f);
-                        const float4 v = integrate_force(kp, vel[o], f);
+                        const float4 v = integrate_force(kp, v_o, f);
                         vel[o] = v;
                         force[o] = kp.gravity;
-                        pos[o] = integrate_velocity(kp, pos[o], v);
+                        pos[o] = integrate_velocity(kp, p_o, v);
                     } else {
                         force[o] = f;
                     }

@@ -54,6 +54,10 @@ def lib() -> C.CDLL:
             "orc_step": (C.c_int, [P, P, P, U, P, P, P, P, P, P, P, C.c_int]),
             "orc_step_f64": (C.c_int, [P, P, P, P, U, P, P, P, P, P, P, P]),
             "orc_num_threads": (C.c_int, []),
+            "orc2d_default_params": (None, [P]),
+            "orc2d_table_size": (U, [P]),
+            "orc2d_compute_border": (None, [P, C.c_int, C.c_int, P, P, P]),
+            "orc2d_step": (None, [P, U, P, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P]),
             "orc_set_num_threads": (None, [C.c_int]),
         }
         for name, (res, args) in sig.items():
@@ -197,3 +201,44 @@ def front_end(pos, vel, params):
     spos, svel = reorder(index, pos, vel)
     cs, ce = find_bounds(cell, table_cells(params))
     return cell, index, spos, svel, cs, ce
+
+
+class Step2D:
+    """Everything one oclFluid2D::compute leaves behind."""
+
+    def __init__(self, n: int, table: int):
+        self.cell = np.empty(n, np.uint32)
+        self.index = np.empty(n, np.uint32)
+        self.sorted = np.empty((n, 6), np.float32)
+        self.pstate = np.empty((n, 4), np.float32)
+        self.relaxed = np.empty((n, 2), np.float32)
+        self.prev = np.empty((n, 2), np.float32)
+        self.cell_start = np.empty(table, np.uint32)
+        self.cell_end = np.empty(table, np.uint32)
+
+
+def default_params_2d(p) -> None:
+    lib().orc2d_default_params(_pp(p))
+
+
+def table_size_2d(p) -> int:
+    return int(lib().orc2d_table_size(_pp(p)))
+
+
+def compute_border_2d(mask: np.ndarray, p):
+    """clComputeBorder on a [H, W, 4] float32 mask; returns (vector, state) [H, W, 4]."""
+    h, w = mask.shape[:2]
+    vec = np.empty((h, w, 4), np.float32)
+    st = np.empty((h, w, 4), np.float32)
+    lib().orc2d_compute_border(_p(np.ascontiguousarray(mask, np.float32)), w, h, _pp(p), _p(vec), _p(st))
+    return vec, st
+
+
+def step_2d(state: np.ndarray, p, border_state: np.ndarray, border_vec: np.ndarray) -> Step2D:
+    """One FP32 step of oclFluid2D::compute; state is float32 [N, 6] (updated in place)."""
+    n = state.shape[0]
+    h, w = border_state.shape[:2]
+    r = Step2D(n, table_size_2d(p))
+    lib().orc2d_step(_p(state), n, _pp(p), _p(border_state), _p(border_vec), w, h, _p(r.cell), _p(r.index),
+                     _p(r.sorted), _p(r.pstate), _p(r.relaxed), _p(r.prev), _p(r.cell_start), _p(r.cell_end))
+    return r
