@@ -2,7 +2,7 @@
 """SPH particle-steps/s of the 3D block collapse (1,048,576 particles) on one GB300.
 
 One "step" is one oclFluid3D::compute() of the whole scene: hash, one-sweep sort (+reorder),
-cell bounds, density, forces + integration. Default: N=1 GPU, 1000 timed steps after 5
+cell bounds, density, forces + integration. Default: N=1 GPU, 500 timed steps after 5
 warm-up steps, L2 flushed (512 MiB write) between timed steps, each step timed with CUDA
 events on the stream it runs on. Prints one JSON line.
 
@@ -162,6 +162,132 @@ def cpu_baseline(scene, seconds: float = 10.0):
             "sample": f"{steps} full steps of the {scene.n}-particle scene ({dt:.1f} s)"}
 
 
+def _time_steps(fn, steps: int, stream) -> float:
+    """Device milliseconds of `steps` calls of fn(), CUDA events on `stream`."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def extra_batched(stream, steps: int = 10) -> dict:
+    """256 independent scenes (log-uniform 4,096-262,144 particles): one batched step vs the
+    plain step looped over the same scenes."""
+    import torch
+    from libcl_gb300 import BUF_FORCE, BUF_POSITION, BUF_VELOCITY, Batch3D, Fluid3D
+    from libcl_gb300.scenes import batched_ensemble
+    b = batched_ensemble()
+    bt = Batch3D()
+    bt.set_scenes(b.shared, b.descs)
+    bt.buffer(BUF_POSITION).copy_(torch.from_numpy(b.pos))
+    bt.buffer(BUF_VELOCITY).zero_()
+    bt.buffer(BUF_FORCE).zero_()
+    best_w = bt.autotune(stream)
+    for _ in range(3):
+        bt.compute(stream)
+    t_b = _time_steps(lambda: bt.compute(stream), steps, stream)
+    assert bt.sync_status() == 0
+    del bt
+    fluids = []
+    for s in range(len(b.descs)):
+        f = Fluid3D()
+        load_scene(f, b.scene(s))
+        fluids.append(f)
+    for _ in range(3):
+        for f in fluids:
+            f.compute(stream)
+    t_l = _time_steps(lambda: [f.compute(stream) for f in fluids], max(2, steps // 2), stream)
+    looped = b.n * max(2, steps // 2) / (t_l * 1e-3)
+    batched = b.n * steps / (t_b * 1e-3)
+    return {"scenes": len(b.descs), "particles": b.n, "brick_width": best_w,
+            "batched_particle_steps_per_s": batched, "looped_particle_steps_per_s": looped,
+            "speedup": batched / looped, "batched_ms_per_step": t_b / steps}
+
+
+def extra_sort(stream) -> dict:
+    """16,777,216 (key, index) pairs: uniform 32-bit keys and Morton keys of a jittered lattice
+    (0-20 particles per occupied cell, 2^22-cell table) + cell start/end extraction."""
+    import torch
+    from libcl_gb300 import RadixSort
+    from libcl_gb300.scenes import SplitMix64
+    n = 1 << 24
+    rng = SplitMix64(3)
+    uni = torch.from_numpy((rng.next_u64(n) >> np.uint64(32)).astype(np.uint32).view(np.int32)).cuda()
+    counts = (SplitMix64(4).next_u64(1 << 22) % np.uint64(21)).astype(np.int64)
+    cells = np.nonzero(np.cumsum(counts) <= n)[0]
+    cid = np.repeat(cells, counts[cells])
+
+    def spread(v):
+        v = v.astype(np.uint64) & np.uint64(0x3FF)
+        for sh, m in ((16, 0x030000FF), (8, 0x0300F00F), (4, 0x030C30C3), (2, 0x09249249)):
+            v = (v | (v << np.uint64(sh))) & np.uint64(m)
+        return v
+    mort = (spread(cid % 128) | (spread((cid // 128) % 128) << np.uint64(1)) | (spread(cid // 16384) << np.uint64(2)))
+    mort = mort.astype(np.uint32)[np.argsort(SplitMix64(5).next_u64(cid.size), kind="stable")]
+    mor = torch.from_numpy(mort.view(np.int32)).cuda()
+    sorter = RadixSort()
+    out = {}
+    for name, keys, bits in (("uniform32", uni, 32), ("morton24", mor, 24)):
+        vals = torch.arange(keys.numel(), dtype=torch.int32, device="cuda")
+        k, v = keys.clone(), vals.clone()
+        sorter.compute(k, v, 0, bits, stream)  # warm-up (allocates)
+        reps = 5
+        ts = []
+        for _ in range(reps):
+            k.copy_(keys)
+            v.copy_(vals)
+            ts.append(_time_steps(lambda: sorter.compute(k, v, 0, bits, stream), 1, stream))
+        ms = statistics.median(ts)
+        out[name] = {"pairs": keys.numel(), "ms": ms, "pairs_per_s": keys.numel() / (ms * 1e-3),
+                     "hbm_gbs_algorithmic": (4 + 16 * ((bits + 7) // 8)) * keys.numel() / (ms * 1e-3) / 1e9}
+    cs = torch.empty(1 << 22, dtype=torch.int32, device="cuda")
+    ce = torch.empty(1 << 22, dtype=torch.int32, device="cuda")
+    ms = _time_steps(lambda: sorter.cell_bounds(k, cs, ce, stream), 5, stream) / 5
+    out["cell_bounds_2^22_ms"] = ms
+    assert sorter.sync_status() == 0
+    return out
+
+
+def extra_2d(stream, steps: int = 500) -> dict:
+    """The 2D dam break (16,384 particles, poly6/spiky on the 3D step with dims = 2) and the
+    reference's own 2D relaxation model (oclFluid2D, 16,384 particles)."""
+    import torch
+    from libcl_gb300 import Fluid2D, Fluid3D
+    from libcl_gb300.scenes import dam_break_2d
+    sc = dam_break_2d()
+    f = Fluid3D()
+    load_scene(f, sc)
+    for _ in range(5):
+        f.compute(stream)
+    t = _time_steps(lambda: f.compute(stream), steps, stream)
+    assert f.sync_status() == 0
+    out = {"dam_break_poly6_2d": {"particles": sc.n, "ms_per_step": t / steps,
+                                  "particle_steps_per_s": sc.n * steps / (t * 1e-3)}}
+    g = Fluid2D()
+    g.compile()
+    n = g.getParticleCount()
+    st = np.zeros((n, 6), np.float32)
+    side = int(np.sqrt(n))
+    iy, ix = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
+    st[:, 0], st[:, 1], st[:, 4] = 1.0 + ix.ravel() * 0.06, 1.0 + iy.ravel() * 0.06, 0.7
+    g.getStateBuffer().copy_(torch.from_numpy(st))
+    mask = np.zeros((256, 256, 4), np.float32)
+    mask[:8, :, 3] = mask[-8:, :, 3] = mask[:, :8, 3] = mask[:, -8:, 3] = 1
+    g.computeBorder(torch.from_numpy(mask).cuda(), stream)
+    for _ in range(5):
+        g.compute(stream)
+    t = _time_steps(lambda: g.compute(stream), steps, stream)
+    assert g.sync_status() == 0
+    out["reference_relaxation_2d"] = {"particles": n, "ms_per_step": t / steps,
+                                      "particle_steps_per_s": n * steps / (t * 1e-3)}
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU port of the reference kernels on a bounded sample."""
     if rank != 0:
@@ -197,12 +323,13 @@ def run_reference(args, rank, world):
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--quick", action="store_true", help="skip e2e/profile/baseline legs (for ncu)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched / sort / 2D side measurements")
     ap.add_argument("--brick-width", type=int, default=0, help="cells per neighbour brick (0: library default)")
     args = ap.parse_args(argv)
     rank, world, local = env_rank()
@@ -332,6 +459,11 @@ def main(argv=None) -> int:
         result["e2e"] = {"value": scene.n * k_e2e / (e2e_ms * 1e-3), "unit": UNIT,
                          "h2d_bytes_per_step": 3 * 16 * scene.n, "d2h_bytes_per_step": 3 * 16 * scene.n,
                          "steps": k_e2e}
+        if not args.no_extras:
+            del fluid, flush
+            torch.cuda.empty_cache()
+            result["extras"] = {"batched_256_scenes": extra_batched(stream), "sort_16m": extra_sort(stream),
+                                "two_d": extra_2d(stream)}
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
     if rank == 0:

@@ -92,7 +92,7 @@ GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h);
  * gbsph_radix_sort_compute for callers that cannot allocate device memory (a host framework
  * that owns all device memory through its own allocator, real-time loops that must not stall
  * on cudaMalloc/cudaFree, plugins with a fixed memory footprint). Its scratch is a static
- * device array of about 4.5 MB that every GPU loading the library holds until exit.
+ * device array of about 5 MB that every GPU loading the library holds until exit.
  * Limits: at most 262,144 pairs (GBSPH_ERR_TOO_LARGE beyond); the first call on a device
  * looks up the array's address, so make it before any stream capture; all calls share the
  * array, so calls that overlap on the GPU race; device-side timeouts are not reported. */
@@ -239,6 +239,47 @@ GBSPH_API int gbsph_fluid3d_sync_status(gbsph_fluid3d_t h, void* stream);
  * getEndTime (libCL/oclKernel.cpp:167-202). */
 GBSPH_API int gbsph_fluid3d_stage_times(gbsph_fluid3d_t h, float* ms, int max_stages);
 GBSPH_API const char* gbsph_fluid3d_last_error(gbsph_fluid3d_t h);
+
+/* ------------------------------------------------------------------------------------------
+ * Batched 3D scenes (no counterpart in the reference, which advances one oclFluid3D per
+ * compute()): many independent LINEAR_GRID scenes of uneven particle counts, each with its own
+ * gas constant, viscosity, clip box and grid, advanced together by one launch per stage of the
+ * step (hash, sort passes, bounds, density, forces + integration), replayed as one CUDA graph.
+ * Scene s owns particles [first_s, first_s + n_s) of the concatenated float4 arrays (in the
+ * order the scenes were given) and never interacts with another scene.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbsph_scene3d_desc {
+    uint32_t n_particles;
+    float stiffness;      /* gas constant k of p = p0 + k (rho - rho0) */
+    float viscosity;      /* mu; the viscosity constant is mu * 45 / (pi h^6) */
+    float boxMin[3];
+    float boxMax[3];
+    float gridOrigin[3];
+    int32_t gridDim[3];
+} gbsph_scene3d_desc;
+
+typedef struct gbsph_batch3d_s* gbsph_batch3d_t;
+
+GBSPH_API int gbsph_batch3d_create(gbsph_batch3d_t* out);
+GBSPH_API int gbsph_batch3d_destroy(gbsph_batch3d_t h);
+/* Defines the scenes. `shared` supplies deltaTime, particleRadius, cellSize, mass, pressure,
+ * density, kernelConstant, pressureConstant, velocitylimit, gravity and dims (3); stiffness,
+ * viscosity, box and grid come from each scene. Allocates every buffer (zeroed). */
+GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_params* shared,
+                                       const gbsph_scene3d_desc* scenes, int n_scenes);
+/* Concatenated buffers (GBSPH_BUF_*), `count` = total particles. */
+GBSPH_API void* gbsph_batch3d_get_buffer(gbsph_batch3d_t h, int which, size_t* count);
+/* First particle and particle count of scene `s`. */
+GBSPH_API int gbsph_batch3d_scene_range(gbsph_batch3d_t h, int s, size_t* first, size_t* count);
+/* GBSPH_OPT_CUDA_GRAPH, GBSPH_OPT_BRICK_WIDTH. */
+GBSPH_API int gbsph_batch3d_set_option(gbsph_batch3d_t h, int option, int value);
+/* One step of every scene, asynchronous on `stream`. */
+GBSPH_API int gbsph_batch3d_compute(gbsph_batch3d_t h, void* stream);
+/* Times the step for brick widths 4, 8 and 16 on the current state (which is saved and
+ * restored), keeps the fastest and returns it through best_width. Synchronises `stream`. */
+GBSPH_API int gbsph_batch3d_autotune(gbsph_batch3d_t h, void* stream, int* best_width);
+GBSPH_API int gbsph_batch3d_sync_status(gbsph_batch3d_t h, void* stream);
+GBSPH_API const char* gbsph_batch3d_last_error(gbsph_batch3d_t h);
 
 /* ------------------------------------------------------------------------------------------
  * 2D SPH fluid: the reference's double-density relaxation model with an image-sampled wall

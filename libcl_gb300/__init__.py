@@ -63,6 +63,13 @@ class Fluid2DParams(C.Structure):
 (BUF2D_STATE, BUF2D_SORTED_STATE, BUF2D_INDEX, BUF2D_CELL, BUF2D_PRESSURE, BUF2D_RELAXED, BUF2D_PREVIOUS,
  BUF2D_BORDER_STATE, BUF2D_BORDER_VECTOR) = range(9)
 
+class SceneDesc(C.Structure):
+    """gbsph_scene3d_desc: one scene of a batch."""
+    _fields_ = [("n_particles", C.c_uint32), ("stiffness", C.c_float), ("viscosity", C.c_float),
+                ("boxMin", C.c_float * 3), ("boxMax", C.c_float * 3), ("gridOrigin", C.c_float * 3),
+                ("gridDim", C.c_int32 * 3)]
+
+
 HOOK_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)
 LOG_FN = C.CFUNCTYPE(None, C.c_int, C.c_char_p, C.c_void_p)
 
@@ -97,6 +104,16 @@ SIGNATURES = {
     "gbsph_fluid3d_sync_status": (_I, [_P, _P]),
     "gbsph_fluid3d_last_error": (C.c_char_p, [_P]),
     "gbsph_fluid3d_stage_times": (_I, [_P, C.POINTER(C.c_float), _I]),
+    "gbsph_batch3d_create": (_I, [C.POINTER(_P)]),
+    "gbsph_batch3d_destroy": (_I, [_P]),
+    "gbsph_batch3d_set_scenes": (_I, [_P, C.POINTER(Fluid3DParams), C.POINTER(SceneDesc), _I]),
+    "gbsph_batch3d_get_buffer": (_P, [_P, _I, C.POINTER(_SZ)]),
+    "gbsph_batch3d_scene_range": (_I, [_P, _I, C.POINTER(_SZ), C.POINTER(_SZ)]),
+    "gbsph_batch3d_set_option": (_I, [_P, _I, _I]),
+    "gbsph_batch3d_compute": (_I, [_P, _P]),
+    "gbsph_batch3d_autotune": (_I, [_P, _P, C.POINTER(_I)]),
+    "gbsph_batch3d_sync_status": (_I, [_P, _P]),
+    "gbsph_batch3d_last_error": (C.c_char_p, [_P]),
     "gbsph_fluid2d_create": (_I, [C.POINTER(_P)]),
     "gbsph_fluid2d_destroy": (_I, [_P]),
     "gbsph_fluid2d_compile": (_I, [_P]),
@@ -339,6 +356,61 @@ class Fluid3D:
         if n < 0:
             raise GbsphError(n, self.last_error())
         return {STAGE_TIME_NAMES[i]: float(buf[i]) for i in range(n)}
+
+
+class Batch3D:
+    """Many independent 3D scenes advanced together (gbsph_batch3d_*)."""
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_batch3d_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_batch3d_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_batch3d_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_batch3d_last_error(self._h).decode())
+
+    def set_scenes(self, shared: Fluid3DParams, scenes) -> None:
+        arr = (SceneDesc * len(scenes))(*scenes)
+        self._check(self._lib.gbsph_batch3d_set_scenes(self._h, C.byref(shared), arr, len(scenes)))
+
+    def scene_range(self, s: int):
+        first, count = C.c_size_t(), C.c_size_t()
+        self._check(self._lib.gbsph_batch3d_scene_range(self._h, s, C.byref(first), C.byref(count)))
+        return first.value, count.value
+
+    def buffer(self, which: int):
+        import torch
+        count = C.c_size_t()
+        p = self._lib.gbsph_batch3d_get_buffer(self._h, which, C.byref(count))
+        if not p:
+            raise GbsphError(ERR_ARGUMENT, f"no buffer {which}")
+        n = count.value
+        if which in (BUF_INDEX, BUF_CELL):
+            return _device_view(p, n, torch.int32, (n,))
+        return _device_view(p, n * 4, torch.float32, (n, 4))
+
+    def set_option(self, option: int, value: int) -> None:
+        self._check(self._lib.gbsph_batch3d_set_option(self._h, option, value))
+
+    def compute(self, stream=None) -> None:
+        self._check(self._lib.gbsph_batch3d_compute(self._h, _stream(stream)))
+
+    def autotune(self, stream=None) -> int:
+        best = C.c_int()
+        self._check(self._lib.gbsph_batch3d_autotune(self._h, _stream(stream), C.byref(best)))
+        return best.value
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_batch3d_sync_status(self._h, _stream(stream))
 
 
 class Fluid2D:

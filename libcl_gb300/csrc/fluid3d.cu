@@ -17,9 +17,6 @@ using namespace gbsph;
 
 namespace {
 
-constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * CELL_LIST_MAX * 2 +
-                                (size_t)BRICK_WARPS * 32 * WLIST_STRIDE * 2;
-constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
 
 struct DevBuf {
     void* ptr = nullptr;
@@ -346,8 +343,8 @@ int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
         kern<<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp,
                                                                  h->nbr, h->nbr_flag, h->err);
     };
-    if (kp.dims == 2) launch(k_density_brick<2>);
-    else launch(k_density_brick<3>);
+    if (kp.dims == 2) launch(k_density_brick<2, false>);
+    else launch(k_density_brick<3, false>);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
@@ -359,11 +356,11 @@ int st_force_brick(H* h, const KParams& kp, cudaStream_t s, bool fused) {
                                                                 h->nbr_flag, h->err);
     };
     if (kp.dims == 2) {
-        if (fused) launch(k_force_brick<2, true>);
-        else launch(k_force_brick<2, false>);
+        if (fused) launch(k_force_brick<2, true, false>);
+        else launch(k_force_brick<2, false, false>);
     } else {
-        if (fused) launch(k_force_brick<3, true>);
-        else launch(k_force_brick<3, false>);
+        if (fused) launch(k_force_brick<3, true, false>);
+        else launch(k_force_brick<3, false, false>);
     }
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
@@ -472,15 +469,15 @@ int setup_kernels(H* h) {
     const int sms = num_sms();
     int nb = 0;
     const int dsm = (int)DENSITY_SMEM, fsm = (int)FORCE_SMEM;
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_brick<3>, BRICK_THREADS, DENSITY_SMEM));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_brick<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<3, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_brick<2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_brick<3, false>, BRICK_THREADS, DENSITY_SMEM));
     h->dens_blocks = std::max(1, nb) * sms;
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true>, BRICK_THREADS, FORCE_SMEM));
+    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true, false>, BRICK_THREADS, FORCE_SMEM));
     h->force_blocks = std::max(1, nb) * sms;
     return GBSPH_OK;
 }

@@ -27,6 +27,15 @@ constexpr int BRICK_WARPS = BRICK_THREADS / 32;
 constexpr int BRICK_W_MAX = 16;
 constexpr int BRICK_SLOTS = BRICK_W_MAX + 2;
 
+// One scene of a batch (LINEAR_GRID): its particles, cells and bricks are consecutive ranges
+// of the batch's arrays, and its gas constant, viscosity, box and grid are its own.
+struct SceneDev {
+    uint32_t part_off, cell_off, brick_off, n;
+    int nx, ny, nz, bxn;
+    float4 origin, box_min, box_max;
+    float stiff, cvisc, pad0, pad1;
+};
+
 // Kernel-side parameters, passed by value.
 struct KParams {
     float dt, radius, h, mass, p0, rho0, stiff, cvisc, cpress, kconst, vlimit;
@@ -39,7 +48,22 @@ struct KParams {
     int bw, bxn;  // brick width (cells) and bricks per x row
     uint32_t n;
     uint32_t table_cells;
+    const SceneDev* scenes;  // batches only: n_scenes entries, sorted by part/cell/brick offsets
+    int n_scenes;
 };
+
+// Index of the scene whose range [off, next off) holds v (binary search over `n` scenes).
+template <int FIELD>
+__device__ __forceinline__ int scene_of(const SceneDev* __restrict__ sc, int n, uint32_t v) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const uint32_t o = FIELD == 0 ? sc[mid].part_off : (FIELD == 1 ? sc[mid].cell_off : sc[mid].brick_off);
+        if (o <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 // ---- keys ---------------------------------------------------------------------------------
 
@@ -110,7 +134,7 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos, KP
 
 // clReorder (libCL/phys/oclFluid3D.cl:66-72), used when the gather is not fused into the
 // last sort pass.
-__global__ void k_reorder(const uint32_t* __restrict__ index, const float4* __restrict__ pos,
+static __global__ void k_reorder(const uint32_t* __restrict__ index, const float4* __restrict__ pos,
                           const float4* __restrict__ vel, float4* __restrict__ spos,
                           float4* __restrict__ svel, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -122,7 +146,7 @@ __global__ void k_reorder(const uint32_t* __restrict__ index, const float4* __re
 
 // Cell bounds into the interleaved LINEAR_GRID table, plus the list of occupied bricks
 // (brick id = x/W + bxn*(y + ny*z)), appended through an atomic counter.
-__global__ void k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
+static __global__ void k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
                                 uint2* __restrict__ table, uint32_t* __restrict__ bricks,
                                 uint32_t* __restrict__ n_bricks, uint32_t* err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,8 +166,67 @@ __global__ void k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
     if (bid != pbid) bricks[atomicAdd(n_bricks, 1u)] = bid;
 }
 
+// Batch version of k_hash: each particle keys into its own scene's grid; the key is the
+// scene's cell offset plus the local linear key.
+template <bool CLEAR>
+__global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ pos, KParams kp,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                                                    const uint32_t* __restrict__ prev_keys, uint2* __restrict__ table) {
+    __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
+    for (int i = threadIdx.x; i < SORT_MAX_PASSES * SORT_RADIX; i += blockDim.x) s_h[i] = 0;
+    __syncthreads();
+    const int passes = sort_passes(0, kp.end_bit);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kp.n; i += gridDim.x * blockDim.x) {
+        const SceneDev& d = kp.scenes[scene_of<0>(kp.scenes, kp.n_scenes, i)];
+        const float4 p = pos[i];
+        const int gx = (int)floorf(__fdiv_rn(__fsub_rn(p.x, d.origin.x), kp.h));
+        const int gy = (int)floorf(__fdiv_rn(__fsub_rn(p.y, d.origin.y), kp.h));
+        const int gz = (int)floorf(__fdiv_rn(__fsub_rn(p.z, d.origin.z), kp.h));
+        const uint32_t k = d.cell_off + (uint32_t)clampi(gx, 0, d.nx - 1) +
+                           (uint32_t)d.nx * ((uint32_t)clampi(gy, 0, d.ny - 1) + (uint32_t)d.ny * (uint32_t)clampi(gz, 0, d.nz - 1));
+        keys[i] = k;
+        for (int q = 0; q < passes; ++q) {
+            const int shift = q * SORT_RADIX_BITS;
+            const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
+            atomicAdd(&s_h[q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
+        }
+        if (CLEAR) {
+            const uint32_t pk = prev_keys[i];
+            if ((i == 0 || prev_keys[i - 1] != pk) && pk < kp.table_cells) table[pk] = make_uint2(EMPTY, EMPTY);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * SORT_RADIX; i += blockDim.x)
+        if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
+}
+
+__device__ __forceinline__ uint32_t batch_brick_of(const KParams& kp, uint32_t k) {
+    const SceneDev& d = kp.scenes[scene_of<1>(kp.scenes, kp.n_scenes, k)];
+    const uint32_t local = k - d.cell_off, nx = (uint32_t)d.nx;
+    return d.brick_off + (local % nx) / (uint32_t)kp.bw + (uint32_t)d.bxn * (local / nx);
+}
+
+// Batch version of k_bounds_linear: brick ids are global (scene brick offset + local id).
+static __global__ void k_bounds_batch(const uint32_t* __restrict__ keys, KParams kp, uint2* __restrict__ table,
+                               uint32_t* __restrict__ bricks, uint32_t* __restrict__ n_bricks, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kp.n) return;
+    const uint32_t k = keys[i];
+    if (k >= kp.table_cells) {
+        atomicOr(err, DEV_ERR_KEY_RANGE);
+        return;
+    }
+    const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
+    const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
+    if (k != prev) table[k].x = i;
+    if (k != next) table[k].y = i + 1;
+    const uint32_t bid = batch_brick_of(kp, k);
+    const uint32_t pbid = prev == EMPTY ? EMPTY : batch_brick_of(kp, prev);
+    if (bid != pbid) bricks[atomicAdd(n_bricks, 1u)] = bid;
+}
+
 // Splits the interleaved table into two arrays (for inspection through the ABI).
-__global__ void k_table_split(const uint2* __restrict__ table, uint32_t cells,
+static __global__ void k_table_split(const uint2* __restrict__ table, uint32_t cells,
                               uint32_t* __restrict__ cs, uint32_t* __restrict__ ce) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cells) return;
@@ -284,17 +367,22 @@ __device__ __forceinline__ void add_wall(float& fa, float& fw, float sign, float
     }
 }
 
-__device__ __forceinline__ float4 clip_box_force(const KParams& kp, float4 pos, float4 vel, float4 f) {
+__device__ __forceinline__ float4 clip_box_force(const KParams& kp, const float4& box_min, const float4& box_max,
+                                                  float4 pos, float4 vel, float4 f) {
     const float r = kp.radius;
-    add_wall(f.y, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.y, kp.box_min.y)), vel.y);
-    add_wall(f.y, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.y, pos.y)), vel.y);
+    add_wall(f.y, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.y, box_min.y)), vel.y);
+    add_wall(f.y, f.w, -1.0f, __fsub_rn(r, __fsub_rn(box_max.y, pos.y)), vel.y);
     if (kp.dims != 2) {
-        add_wall(f.z, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.z, kp.box_min.z)), vel.z);
-        add_wall(f.z, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.z, pos.z)), vel.z);
+        add_wall(f.z, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.z, box_min.z)), vel.z);
+        add_wall(f.z, f.w, -1.0f, __fsub_rn(r, __fsub_rn(box_max.z, pos.z)), vel.z);
     }
-    add_wall(f.x, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.x, kp.box_min.x)), vel.x);
-    add_wall(f.x, f.w, -1.0f, __fsub_rn(r, __fsub_rn(kp.box_max.x, pos.x)), vel.x);
+    add_wall(f.x, f.w, 1.0f, __fsub_rn(r, __fsub_rn(pos.x, box_min.x)), vel.x);
+    add_wall(f.x, f.w, -1.0f, __fsub_rn(r, __fsub_rn(box_max.x, pos.x)), vel.x);
     return f;
+}
+
+__device__ __forceinline__ float4 clip_box_force(const KParams& kp, float4 pos, float4 vel, float4 f) {
+    return clip_box_force(kp, kp.box_min, kp.box_max, pos, vel, f);
 }
 
 // clIntegrateForce (libCL/phys/oclFluid3D.cl:258-271): clamp |F|, v += F*dt on 4 lanes.
@@ -321,7 +409,7 @@ __device__ __forceinline__ float4 integrate_velocity(const KParams& kp, float4 p
                        __fadd_rn(p.z, __fmul_rn(v.z, kp.dt)), __fadd_rn(p.w, __fmul_rn(v.w, kp.dt)));
 }
 
-__global__ void k_clip_box(const float4* __restrict__ spos, const float4* __restrict__ svel,
+static __global__ void k_clip_box(const float4* __restrict__ spos, const float4* __restrict__ svel,
                            float4* __restrict__ force, const uint32_t* __restrict__ index, KParams kp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
@@ -329,19 +417,19 @@ __global__ void k_clip_box(const float4* __restrict__ spos, const float4* __rest
     force[o] = clip_box_force(kp, spos[i], svel[i], force[o]);
 }
 
-__global__ void k_integrate_force(float4* __restrict__ vel, const float4* __restrict__ force, KParams kp) {
+static __global__ void k_integrate_force(float4* __restrict__ vel, const float4* __restrict__ force, KParams kp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     vel[i] = integrate_force(kp, vel[i], force[i]);
 }
 
-__global__ void k_gravity(float4* __restrict__ force, KParams kp) {  // clGravity, :294-298
+static __global__ void k_gravity(float4* __restrict__ force, KParams kp) {  // clGravity, :294-298
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     force[i] = kp.gravity;
 }
 
-__global__ void k_integrate_velocity(float4* __restrict__ pos, const float4* __restrict__ vel, KParams kp) {
+static __global__ void k_integrate_velocity(float4* __restrict__ pos, const float4* __restrict__ vel, KParams kp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     pos[i] = integrate_velocity(kp, pos[i], vel[i]);
@@ -349,7 +437,7 @@ __global__ void k_integrate_velocity(float4* __restrict__ pos, const float4* __r
 
 // clip + integrate-force + gravity + integrate-velocity in one pass over sorted slots.
 // Equivalent to the four reference kernels because index is a permutation.
-__global__ void k_post_fused(const float4* __restrict__ spos, const float4* __restrict__ svel,
+static __global__ void k_post_fused(const float4* __restrict__ spos, const float4* __restrict__ svel,
                              const uint32_t* __restrict__ index, float4* __restrict__ pos,
                              float4* __restrict__ vel, float4* __restrict__ force, KParams kp) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -374,33 +462,69 @@ struct BrickShared {
     uint32_t total;
     uint32_t brick;
     uint32_t abort;
+    // the brick's scene: grid, cell-table offset and the parameters that vary per scene
+    int nx, ny, nz, bxn;
+    uint32_t cell_off, lbrick;  // lbrick: the brick's id within its scene
+    float stiff, cvisc;
+    float4 box_min, box_max;
     unsigned long long bar;
 };
 
-// Loads the brick's geometry and neighbour-row ranges into S; thread 0 starts the bulk copies
-// of `n_arrays` float4 arrays (pos, optionally vel) when the rows fit in `cap`.
-// Returns the brick's first cell x and cell count through x0/ncell.
-template <int DIMS>
+// Loads the brick's scene, geometry and neighbour-row ranges into S. A single scene takes its
+// grid and parameters from kp; in a batch (BATCH) the brick id is global and its scene is
+// found in kp.scenes. Returns the brick's first cell x and cell count through x0/ncell.
+template <int DIMS, bool BATCH>
 __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, uint32_t bid,
                                             const uint2* __restrict__ table, uint32_t* err, int& x0,
                                             int& ncell) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     const int W = kp.bw;
-    const int bx = (int)(bid % (uint32_t)kp.bxn);
-    const uint32_t yz = bid / (uint32_t)kp.bxn;
-    const int y = (int)(yz % (uint32_t)kp.ny);
-    const int z = (int)(yz / (uint32_t)kp.ny);
-    x0 = bx * W;
-    ncell = min(W, kp.nx - x0);
     const int t = threadIdx.x;
+    if (t == 0) {
+        if (BATCH) {
+            const int sc = scene_of<2>(kp.scenes, kp.n_scenes, bid);
+            const SceneDev& d = kp.scenes[sc];
+            S.nx = d.nx;
+            S.ny = d.ny;
+            S.nz = d.nz;
+            S.bxn = d.bxn;
+            S.cell_off = d.cell_off;
+            S.stiff = d.stiff;
+            S.cvisc = d.cvisc;
+            S.box_min = d.box_min;
+            S.box_max = d.box_max;
+            S.lbrick = bid - d.brick_off;
+        } else {
+            S.nx = kp.nx;
+            S.ny = kp.ny;
+            S.nz = kp.nz;
+            S.bxn = kp.bxn;
+            S.cell_off = 0;
+            S.stiff = kp.stiff;
+            S.cvisc = kp.cvisc;
+            S.box_min = kp.box_min;
+            S.box_max = kp.box_max;
+            S.lbrick = bid;
+        }
+    }
+    __syncthreads();
+    const uint32_t lb = S.lbrick;
+    const int nx = S.nx, ny = S.ny, nz = S.nz;
+    const int bx = (int)(lb % (uint32_t)S.bxn);
+    const uint32_t yz = lb / (uint32_t)S.bxn;
+    const int y = (int)(yz % (uint32_t)ny);
+    const int z = (int)(yz / (uint32_t)ny);
+    x0 = bx * W;
+    ncell = min(W, nx - x0);
+    const uint2* tab = table + S.cell_off;
     for (int idx = t; idx < R * (W + 2); idx += BRICK_THREADS) {
         const int r = idx / (W + 2), c = idx - r * (W + 2);
         const int cy = y + (r % 3) - 1;
         const int cz = DIMS == 3 ? z + (r / 3) - 1 : 0;
         const int cx = x0 - 1 + c;
         uint32_t cnt = 0, st = 0;
-        if (cx >= 0 && cx < kp.nx && cy >= 0 && cy < kp.ny && cz >= 0 && cz < kp.nz) {
-            const uint2 e = table[(uint32_t)cx + (uint32_t)kp.nx * ((uint32_t)cy + (uint32_t)kp.ny * (uint32_t)cz)];
+        if (cx >= 0 && cx < nx && cy >= 0 && cy < ny && cz >= 0 && cz < nz) {
+            const uint2 e = tab[(uint32_t)cx + (uint32_t)nx * ((uint32_t)cy + (uint32_t)ny * (uint32_t)cz)];
             if (e.x != EMPTY) {
                 cnt = e.y - e.x;
                 st = e.x;
@@ -493,6 +617,12 @@ constexpr uint16_t NBR_END = 0xFFFFu;    // terminates a lane's neighbour sub-li
 constexpr uint32_t WLIST_STRIDE = NBR_CAP + 2;  // shared-memory stride per target (33 words: no bank conflicts)
 constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists the force kernel stages
 
+
+// Dynamic shared memory of the brick kernels.
+constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * CELL_LIST_MAX * 2 +
+                                (size_t)BRICK_WARPS * 32 * WLIST_STRIDE * 2;
+constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
+
 // Slots of each lane's sub-list when Q lanes share a target: a multiple of 8 (one 16-byte
 // vector) when Q <= 8, else 4 or 2, so sub-lists start on their load width.
 __device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
@@ -509,7 +639,7 @@ __device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
 // index of every candidate. Each lane records its in-range neighbours (r^2 > 0) as staged
 // indices in its own sub-list of nbr[gi][NBR_CAP] (in candidate order, NBR_END-terminated);
 // nbr_flag[gi] = 1 when a sub-list overflowed or the brick could not be staged.
-template <int DIMS>
+template <int DIMS, bool BATCH>
 __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
                                                                  float4* __restrict__ svel,
                                                                  const uint2* __restrict__ table,
@@ -539,7 +669,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
         int x0, ncell;
-        brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
+        brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         const bool staged = brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr);
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
@@ -623,7 +753,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                     float rho = kp.rho0, p = kp.p0;
                     if (cnt > 2.5f) {
                         rho = fmaxf(1.0f, kp.mass * kp.kconst * acc);
-                        p = kp.p0 + kp.stiff * (rho - kp.rho0);
+                        p = kp.p0 + S.stiff * (rho - kp.rho0);
                     }
                     spos[gi] = make_float4(pi.x, pi.y, pi.z, rho);
                     reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
@@ -671,7 +801,7 @@ __device__ __forceinline__ void force_pair(const float4& pi, const float4& vi, f
 // (overflow, unstaged brick) are handled by scanning the rows. With FUSED the clip-box,
 // integrate-force, gravity and integrate-velocity stages follow in registers; otherwise the
 // SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
-template <int DIMS, bool FUSED>
+template <int DIMS, bool FUSED, bool BATCH>
 __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __restrict__ spos,
                                                                const float4* __restrict__ svel,
                                                                const uint32_t* __restrict__ index,
@@ -707,7 +837,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
         int x0, ncell;
-        brick_setup<DIMS>(S, kp, bricks[b], table, err, x0, ncell);
+        brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         // the brick's targets are consecutive particles: stage their lists with the rows
         const uint32_t tfirst = S.lo[RC] + S.off[RC][1];
         const uint32_t ntarg = S.off[RC][ncell + 1] - S.off[RC][1];
@@ -807,12 +937,13 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                 for (int k = 0; k < 6; ++k) acc[k] = reduce_q(acc[k], q, Q, tg);
                 if (active && q == 0) {
                     float4 f = f_o;
-                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(kp.cvisc, acc[3])), kp.mass));
-                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(kp.cvisc, acc[4])), kp.mass));
-                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(kp.cvisc, acc[5])), kp.mass));
+                    const float cvisc = S.cvisc;
+                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(cvisc, acc[3])), kp.mass));
+                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(cvisc, acc[4])), kp.mass));
+                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(cvisc, acc[5])), kp.mass));
                     f.w = 0.0f;
                     if (FUSED) {
-                        f = clip_box_force(kp, pi, vi, f);
+                        f = clip_box_force(kp, S.box_min, S.box_max, pi, vi, f);
                         const float4 v = integrate_force(kp, v_o, f);
                         vel[o] = v;
                         force[o] = kp.gravity;

@@ -48,8 +48,9 @@ int fail(std::string* last_error, int status, const std::string& msg);
 constexpr int SORT_RADIX_BITS = 8;
 constexpr int SORT_RADIX = 1 << SORT_RADIX_BITS;
 constexpr int SORT_THREADS = 256;
-constexpr int SORT_ITEMS = 16;
-constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;
+constexpr int SORT_ITEMS = 16;                              // keys per thread in the largest tile
+constexpr int SORT_TILE = SORT_THREADS * SORT_ITEMS;        // largest tile (4096 keys)
+constexpr int SORT_MIN_TILE = SORT_THREADS * 4;             // smallest tile (1024 keys): sizes the look-back words
 constexpr int SORT_MAX_PASSES = 4;
 constexpr size_t SORT_HEADER_BYTES = 4352;
 constexpr size_t SORT_USER_COUNTER_OFFSET = 4112;  // 60 uint32 free for callers
@@ -58,7 +59,10 @@ constexpr uint32_t SORT_MAX_KEYS = (1u << 30) - 1u;
 __host__ __device__ inline int sort_passes(int start_bit, int end_bit) {
     return (end_bit - start_bit + SORT_RADIX_BITS - 1) / SORT_RADIX_BITS;
 }
-__host__ __device__ inline uint32_t sort_tiles(uint32_t n) { return (n + SORT_TILE - 1) / SORT_TILE; }
+__host__ __device__ inline uint32_t sort_tiles(uint32_t n, uint32_t tile = SORT_MIN_TILE) { return (n + tile - 1) / tile; }
+// Keys per thread of a pass over n keys: small sorts use small tiles (more tiles in flight,
+// shorter per-tile latency), large ones the largest tile (fewer look-back steps).
+inline int sort_items_for(uint32_t n) { return n <= (1u << 21) ? 8 : 16; }
 size_t onesweep_scratch_bytes(uint32_t n, int passes);
 
 // Optional gather fused into the last pass: dst[k][dest] = src[k][value] for k < n_gather.

@@ -80,14 +80,15 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
         if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
 }
 
-template <bool IOTA, int NGATHER>
+template <bool IOTA, int NGATHER, int ITEMS>
 __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
     int bits, int pass, uint32_t tiles, uint32_t* __restrict__ scratch, uint32_t* err,
     SortGather gather) {
-    __shared__ uint32_t s_keys[SORT_TILE];
-    __shared__ uint32_t s_vals[SORT_TILE];
+    constexpr int TILE = SORT_THREADS * ITEMS;
+    __shared__ uint32_t s_keys[TILE];
+    __shared__ uint32_t s_vals[TILE];
     __shared__ uint32_t s_whist[SORT_WARPS * SORT_RADIX];
     __shared__ uint32_t s_tile_start[SORT_RADIX];
     __shared__ uint32_t s_base[SORT_RADIX];
@@ -107,14 +108,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         if (t == 0) atomicOr(err, DEV_ERR_CAPACITY);
         return;
     }
-    const uint32_t base = tile * SORT_TILE;
+    const uint32_t base = tile * TILE;
     const uint32_t mask = (1u << bits) - 1u;
 
     // Load: warp-striped, so item order inside the tile is (warp, i, lane) == index order.
-    uint32_t k[SORT_ITEMS], v[SORT_ITEMS], r[SORT_ITEMS];
+    uint32_t k[ITEMS], v[ITEMS], r[ITEMS];
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; ++i) {
-        const uint32_t idx = base + (uint32_t)(warp * 32 * SORT_ITEMS + i * 32 + lane);
+    for (int i = 0; i < ITEMS; ++i) {
+        const uint32_t idx = base + (uint32_t)(warp * 32 * ITEMS + i * 32 + lane);
         const bool in = idx < n;
         k[i] = in ? keys_in[idx] : 0xFFFFFFFFu;  // padding sorts last in the top digit
         v[i] = IOTA ? idx : (in ? vals_in[idx] : 0u);
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     uint32_t* wh = s_whist + warp * SORT_RADIX;
     const uint32_t lt = lanemask_lt();
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; ++i) {
+    for (int i = 0; i < ITEMS; ++i) {
         const uint32_t d = (k[i] >> shift) & mask;
         uint32_t peers = 0xffffffffu;
         for (int b = 0; b < bits; ++b) {
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
 
     // Tile-local sorted order in shared memory.
 #pragma unroll
-    for (int i = 0; i < SORT_ITEMS; ++i) {
+    for (int i = 0; i < ITEMS; ++i) {
         const uint32_t d = (k[i] >> shift) & mask;
         const uint32_t pos = s_tile_start[d] + s_whist[warp * SORT_RADIX + d] + r[i];
         s_keys[pos] = k[i];
@@ -194,9 +195,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     __syncthreads();
 
     // Each digit's run goes to one contiguous range of the output.
-    const uint32_t valid = min((uint32_t)SORT_TILE, n - base);
+    const uint32_t valid = min((uint32_t)TILE, n - base);
 #pragma unroll 4
-    for (int i = 0; i < SORT_ITEMS; ++i) {
+    for (int i = 0; i < ITEMS; ++i) {
         const uint32_t j = (uint32_t)(i * SORT_THREADS + t);
         if (j < valid) {
             const uint32_t key = s_keys[j], val = s_vals[j];
@@ -235,17 +236,27 @@ __global__ void k_cell_bounds(const uint32_t* __restrict__ keys, uint32_t n,
     if (i == n - 1) ce[k] = n;
 }
 
+template <bool IOTA, int ITEMS>
+cudaError_t launch_pass_items(int ngather, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
+                              uint32_t* vout, uint32_t n, int shift, int bits, int pass, uint32_t* scratch,
+                              uint32_t* err, const SortGather& g, cudaStream_t s) {
+    const uint32_t tiles = sort_tiles(n, SORT_THREADS * ITEMS);
+    if (ngather == 2)
+        k_onesweep<IOTA, 2, ITEMS><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    else if (ngather == 1)
+        k_onesweep<IOTA, 1, ITEMS><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    else
+        k_onesweep<IOTA, 0, ITEMS><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
+    return cudaGetLastError();
+}
+
 template <bool IOTA>
 cudaError_t launch_pass(int ngather, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
-                        uint32_t* vout, uint32_t n, int shift, int bits, int pass, uint32_t tiles,
-                        uint32_t* scratch, uint32_t* err, const SortGather& g, cudaStream_t s) {
-    if (ngather == 2)
-        k_onesweep<IOTA, 2><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
-    else if (ngather == 1)
-        k_onesweep<IOTA, 1><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
-    else
-        k_onesweep<IOTA, 0><<<tiles, SORT_THREADS, 0, s>>>(kin, vin, kout, vout, n, shift, bits, pass, tiles, scratch, err, g);
-    return cudaGetLastError();
+                        uint32_t* vout, uint32_t n, int shift, int bits, int pass, uint32_t* scratch,
+                        uint32_t* err, const SortGather& g, cudaStream_t s) {
+    if (sort_items_for(n) == 8)
+        return launch_pass_items<IOTA, 8>(ngather, kin, vin, kout, vout, n, shift, bits, pass, scratch, err, g, s);
+    return launch_pass_items<IOTA, 16>(ngather, kin, vin, kout, vout, n, shift, bits, pass, scratch, err, g, s);
 }
 
 }  // namespace
@@ -278,7 +289,6 @@ cudaError_t onesweep_histogram(const uint32_t* keys, uint32_t n, int start_bit, 
 cudaError_t onesweep_passes(const OnesweepArgs& a, cudaStream_t s) {
     const int P = sort_passes(a.start_bit, a.end_bit);
     if (a.n == 0 || P == 0) return cudaSuccess;
-    const uint32_t tiles = sort_tiles(a.n);
     const uint32_t* kin = a.keys_in;
     const uint32_t* vin = a.vals_in;
     for (int p = 0; p < P; ++p) {
@@ -289,8 +299,8 @@ cudaError_t onesweep_passes(const OnesweepArgs& a, cudaStream_t s) {
         const int bits = std::min(SORT_RADIX_BITS, a.end_bit - shift);
         const int ng = last ? a.gather.n_gather : 0;
         cudaError_t e = (vin == nullptr)
-            ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, tiles, (uint32_t*)a.scratch, a.err, a.gather, s)
-            : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, tiles, (uint32_t*)a.scratch, a.err, a.gather, s);
+            ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s)
+            : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s);
         if (e != cudaSuccess) return e;
         kin = kout;
         vin = vout;
@@ -482,10 +492,10 @@ GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h) {
 namespace {
 
 constexpr uint32_t NOALLOC_MAX_KEYS = 262144;  // 2^18 pairs
-constexpr size_t NOALLOC_STATUS_BYTES = (size_t)SORT_MAX_PASSES * ((NOALLOC_MAX_KEYS + SORT_TILE - 1) / SORT_TILE) * SORT_RADIX * 4;
+constexpr size_t NOALLOC_STATUS_BYTES = (size_t)SORT_MAX_PASSES * ((NOALLOC_MAX_KEYS + SORT_MIN_TILE - 1) / SORT_MIN_TILE) * SORT_RADIX * 4;
 constexpr size_t NOALLOC_ERR_OFFSET = SORT_HEADER_BYTES + NOALLOC_STATUS_BYTES;  // one uint32 (256 B slot)
 constexpr size_t NOALLOC_TMP_OFFSET = NOALLOC_ERR_OFFSET + 256;
-constexpr size_t NOALLOC_BYTES = NOALLOC_TMP_OFFSET + 4ull * NOALLOC_MAX_KEYS * sizeof(uint32_t);  // ~4.5 MB
+constexpr size_t NOALLOC_BYTES = NOALLOC_TMP_OFFSET + 4ull * NOALLOC_MAX_KEYS * sizeof(uint32_t);  // ~5 MB
 static_assert(SORT_HEADER_BYTES % 256 == 0 && NOALLOC_ERR_OFFSET % 256 == 0, "256-byte aligned regions");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];

@@ -139,3 +139,69 @@ def clone_params(p: Fluid3DParams) -> Fluid3DParams:
     import ctypes
     ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(Fluid3DParams))
     return q
+
+
+@dataclasses.dataclass
+class BatchScenes:
+    """A batch of independent 3D scenes: concatenated float4 state plus per-scene descriptions."""
+    shared: Fluid3DParams
+    descs: list
+    pos: np.ndarray
+    vel: np.ndarray
+    firsts: list
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+    def scene(self, s: int) -> Scene3D:
+        """Scene s as a stand-alone Scene3D (same parameters, same particles)."""
+        d = self.descs[s]
+        p = clone_params(self.shared)
+        p.stiffness = d.stiffness
+        p.viscosity = d.viscosity
+        p.dims = 3
+        params_derive(p)
+        for i in range(3):
+            p.boxMin[i], p.boxMax[i] = d.boxMin[i], d.boxMax[i]
+            p.gridOrigin[i], p.gridDim[i] = d.gridOrigin[i], d.gridDim[i]
+        p.keyMode = KEY_LINEAR_GRID
+        a, n = self.firsts[s], d.n_particles
+        return Scene3D(f"scene{s}", self.pos[a:a + n].copy(), self.vel[a:a + n].copy(), p)
+
+
+def batched_ensemble(n_scenes: int = 256, seed: int = 5, n_min: int = 4096, n_max: int = 262144) -> BatchScenes:
+    """Independent scenes with particle counts drawn log-uniform in [n_min, n_max]: each a
+    near-cubic jittered lattice block (spacing 0.01, h = 0.02, jitter +-0.05h) at the lower
+    corner of its own box, twice the block's extent per axis (a choice of this generator);
+    gas constant uniform in [1, 5], viscosity uniform in [0.01, 0.2]; dt = 5e-5, gravity -9.81
+    along y, rest density 1000, mass 1e-3."""
+    from . import SceneDesc
+    h, sp = 0.02, 0.01
+    rng = SplitMix64(seed)
+    u = rng.uniform(4 * n_scenes).reshape(n_scenes, 4)
+    counts = np.exp(np.log(n_min) + u[:, 0] * (np.log(n_max) - np.log(n_min)))
+    shared = fluid_params(h, sp, 1000.0 * sp ** 3, 1000.0, 3.0, 0.05, 5e-5, (0.0, -9.81, 0.0),
+                          (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), (1, 1, 1))
+    descs, pos_l, firsts, first = [], [], [], 0
+    for s in range(n_scenes):
+        side = max(2, int(round(counts[s] ** (1.0 / 3.0))))
+        nx, ny, nz = side, side, max(1, int(round(counts[s] / (side * side))))
+        p = lattice(nx, ny, nz, sp, (0.5 * sp,) * 3, 0.05 * h, seed * 1000 + s)
+        ext = np.array([nx, ny, nz], np.float64) * sp
+        box = 2.0 * ext
+        d = SceneDesc()
+        d.n_particles = p.shape[0]
+        d.stiffness = float(1.0 + 4.0 * u[s, 1])
+        d.viscosity = float(0.01 + 0.19 * u[s, 2])
+        for i in range(3):
+            d.boxMin[i] = 0.0
+            d.boxMax[i] = float(box[i])
+            d.gridOrigin[i] = 0.0
+            d.gridDim[i] = int(np.ceil(box[i] / h))
+        descs.append(d)
+        pos_l.append(p)
+        firsts.append(first)
+        first += p.shape[0]
+    pos = np.concatenate(pos_l)
+    return BatchScenes(shared, descs, pos, np.zeros_like(pos), firsts)
