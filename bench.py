@@ -288,6 +288,54 @@ def extra_2d(stream, steps: int = 500) -> dict:
     return out
 
 
+def extra_adjoint(stream) -> dict:
+    """Forward + adjoint against forward alone: the differentiable rollout (65,536 particles,
+    200 steps, checkpoint every 20) and the 1M block collapse (20 steps, checkpoint every 10).
+    The adjoint's time covers forward() (the steps plus checkpoints) and backward()
+    (recomputation with recording, then the reverse kernels)."""
+    import torch
+    from libcl_gb300 import Adjoint3D, Fluid3D
+    from libcl_gb300.scenes import block_collapse_3d, differentiable_block
+    out = {}
+    for name, sc, steps, every in (("differentiable_block_64k", differentiable_block(), 200, 20),
+                                   ("block_collapse_1M", block_collapse_3d(), 20, 10)):
+        f = Fluid3D()
+        load_scene(f, sc)
+        grav = torch.tensor(list(sc.params.gravity), dtype=torch.float32, device="cuda")
+        f.getForceBuffer().copy_(grav.expand(sc.n, 4))
+        pos0 = f.getPositionBuffer().clone()
+        vel0 = f.getVelocityBuffer().clone()
+
+        def reset():
+            f.getPositionBuffer().copy_(pos0)
+            f.getVelocityBuffer().copy_(vel0)
+            f.getForceBuffer().copy_(grav.expand(sc.n, 4))
+
+        for _ in range(3):
+            f.compute(stream)
+        reset()
+        t_fwd = _time_steps(lambda: f.compute(stream), steps, stream)
+        adj = Adjoint3D(f, steps, every)
+        gpos = torch.full((sc.n, 4), 1e-6, dtype=torch.float32, device="cuda")
+        gp0, gv0 = torch.empty_like(gpos), torch.empty_like(gpos)
+        gpar = torch.empty(2, dtype=torch.float64, device="cuda")
+        reps = []
+        for _ in range(3):  # the first run captures graphs and warms up
+            reset()
+            t_a = _time_steps(lambda: adj.forward(stream), 1, stream)
+            t_b = _time_steps(lambda: adj.backward_raw(gpos, None, gp0, gv0, gpar, stream), 1, stream)
+            reps.append((t_a, t_b))
+        t_a, t_b = min(reps, key=lambda r: r[0] + r[1])
+        assert f.sync_status() == 0
+        out[name] = {"particles": sc.n, "steps": steps, "checkpoint_every": every,
+                     "forward_ms": t_fwd, "adjoint_forward_ms": t_a, "adjoint_backward_ms": t_b,
+                     "fwd_plus_adj_over_fwd": (t_a + t_b) / t_fwd,
+                     "fwd_plus_adj_particle_steps_per_s": sc.n * steps / ((t_a + t_b) * 1e-3)}
+        del adj, f
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU port of the reference kernels on a bounded sample."""
     if rank != 0:
@@ -463,7 +511,7 @@ def main(argv=None) -> int:
             del fluid, flush
             torch.cuda.empty_cache()
             result["extras"] = {"batched_256_scenes": extra_batched(stream), "sort_16m": extra_sort(stream),
-                                "two_d": extra_2d(stream)}
+                                "two_d": extra_2d(stream), "adjoint": extra_adjoint(stream)}
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
     if rank == 0:

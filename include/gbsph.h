@@ -363,6 +363,37 @@ GBSPH_API int gbsph_fluid2d_get_cell_bounds(gbsph_fluid2d_t h, uint32_t* cell_st
 GBSPH_API int gbsph_fluid2d_sync_status(gbsph_fluid2d_t h, void* stream);
 GBSPH_API const char* gbsph_fluid2d_last_error(gbsph_fluid2d_t h);
 
+/* ------------------------------------------------------------------------------------------
+ * Adjoint of the 3D step (no counterpart in the reference, which has no derivatives):
+ * reverse-mode gradients of a loss on the state after `steps` gbsph_fluid3d_compute() calls
+ * with respect to the initial positions and velocities, the gas constant (stiffness) and the
+ * viscosity. The sort permutation and neighbour sets of each step are held fixed (the integer
+ * sort is not differentiated); the count > 2, max(1, rho), velocity clamp and wall branches are
+ * differentiated on the side the forward step took. Memory: a checkpoint (position, velocity,
+ * force) every `checkpoint_every` steps; backward() recomputes one segment at a time from its
+ * checkpoint, recording 56 bytes per particle per step of that segment.
+ * Requires keyMode GBSPH_KEY_LINEAR_GRID, dims 3 and no integrate hook.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbsph_adjoint3d_s* gbsph_adjoint3d_t;
+
+/* Sized for the fluid's current particle count; the fluid must outlive the adjoint. */
+GBSPH_API int gbsph_adjoint3d_create(gbsph_adjoint3d_t* out, gbsph_fluid3d_t fluid, uint32_t steps,
+                                     uint32_t checkpoint_every);
+GBSPH_API int gbsph_adjoint3d_destroy(gbsph_adjoint3d_t a);
+/* Advances the fluid `steps` steps from its current state (exactly `steps` compute() calls),
+ * keeping the checkpoints. Asynchronous on `stream`. */
+GBSPH_API int gbsph_adjoint3d_forward(gbsph_adjoint3d_t a, void* stream);
+/* After forward(), with the fluid's parameters unchanged: given device float4[n] dL/dposition
+ * and dL/dvelocity of the final state (.w ignored; grad_velocity may be NULL for zero), writes
+ * dL/dposition and dL/dvelocity of the initial state (float4[n], .w = 0; either may be NULL)
+ * and, if grad_params is not NULL, the device doubles grad_params[0] = dL/dstiffness and
+ * grad_params[1] = dL/dviscosity. The fluid is left in the state forward() produced.
+ * Asynchronous on `stream`. */
+GBSPH_API int gbsph_adjoint3d_backward(gbsph_adjoint3d_t a, const float* grad_position,
+                                       const float* grad_velocity, float* grad_position0,
+                                       float* grad_velocity0, double* grad_params, void* stream);
+GBSPH_API const char* gbsph_adjoint3d_last_error(gbsph_adjoint3d_t a);
+
 #ifdef __cplusplus
 }
 #endif

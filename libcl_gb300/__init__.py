@@ -128,6 +128,11 @@ SIGNATURES = {
     "gbsph_fluid2d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
     "gbsph_fluid2d_sync_status": (_I, [_P, _P]),
     "gbsph_fluid2d_last_error": (C.c_char_p, [_P]),
+    "gbsph_adjoint3d_create": (_I, [C.POINTER(_P), _P, C.c_uint32, C.c_uint32]),
+    "gbsph_adjoint3d_destroy": (_I, [_P]),
+    "gbsph_adjoint3d_forward": (_I, [_P, _P]),
+    "gbsph_adjoint3d_backward": (_I, [_P, _P, _P, _P, _P, _P, _P]),
+    "gbsph_adjoint3d_last_error": (C.c_char_p, [_P]),
 }
 
 _lib = None
@@ -356,6 +361,54 @@ class Fluid3D:
         if n < 0:
             raise GbsphError(n, self.last_error())
         return {STAGE_TIME_NAMES[i]: float(buf[i]) for i in range(n)}
+
+
+class Adjoint3D:
+    """Reverse-mode gradients of `steps` Fluid3D.compute() calls (gbsph_adjoint3d_*):
+    forward() advances the fluid keeping a checkpoint every `checkpoint_every` steps;
+    backward(dL/dpos, dL/dvel) returns (dL/dpos0, dL/dvel0, dL/dstiffness, dL/dviscosity)."""
+
+    def __init__(self, fluid: Fluid3D, steps: int, checkpoint_every: int = 20):
+        self._lib = load_library()
+        self.fluid = fluid  # the fluid must outlive the adjoint
+        self.steps = steps
+        h = C.c_void_p()
+        rc = self._lib.gbsph_adjoint3d_create(C.byref(h), fluid.handle, steps, checkpoint_every)
+        if rc:
+            raise GbsphError(rc, "gbsph_adjoint3d_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_adjoint3d_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_adjoint3d_last_error(self._h).decode())
+
+    def last_error(self) -> str:
+        return self._lib.gbsph_adjoint3d_last_error(self._h).decode()
+
+    def forward(self, stream=None) -> None:
+        self._check(self._lib.gbsph_adjoint3d_forward(self._h, _stream(stream)))
+
+    def backward_raw(self, grad_pos, grad_vel=None, grad_pos0=None, grad_vel0=None, grad_params=None,
+                     stream=None) -> int:
+        return self._lib.gbsph_adjoint3d_backward(self._h, _ptr(grad_pos), _ptr(grad_vel), _ptr(grad_pos0),
+                                                  _ptr(grad_vel0), _ptr(grad_params), _stream(stream))
+
+    def backward(self, grad_pos, grad_vel=None, stream=None):
+        """grad_pos / grad_vel: float32 CUDA tensors [N, 4] (.w ignored). Returns
+        (grad_pos0 [N, 4], grad_vel0 [N, 4], grad_params float64 [2] = (d/dstiffness,
+        d/dviscosity)), all on the device."""
+        import torch
+        gp0 = torch.empty_like(grad_pos)
+        gv0 = torch.empty_like(grad_pos)
+        gpar = torch.empty(2, dtype=torch.float64, device=grad_pos.device)
+        self._check(self.backward_raw(grad_pos.contiguous(), None if grad_vel is None else grad_vel.contiguous(),
+                                      gp0, gv0, gpar, stream))
+        return gp0, gv0, gpar
 
 
 class Batch3D:

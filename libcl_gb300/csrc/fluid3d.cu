@@ -11,7 +11,7 @@
 #include <string>
 #include <vector>
 
-#include "fluid3d_kernels.cuh"
+#include "fluid3d_access.h"
 
 using namespace gbsph;
 
@@ -72,6 +72,7 @@ struct gbsph_fluid3d_s {
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
     uint32_t* err = nullptr;
+    float4* rec_force = nullptr;  // set by an adjoint while it records a step
     gbsph_fluid3d_hook_fn hook = nullptr;
     void* hook_user = nullptr;
     int opt_fused = 1, opt_graph = 1, opt_bw = 16, opt_profile = 0;
@@ -178,6 +179,7 @@ KParams make_kparams(const H* h) {
     k.bw = h->opt_bw;
     k.bxn = k.nx > 0 ? (k.nx + k.bw - 1) / k.bw : 0;
     k.n = (uint32_t)h->n;
+    k.rec_force = h->rec_force;
     return k;
 }
 
@@ -483,6 +485,30 @@ int setup_kernels(H* h) {
 }
 
 }  // namespace
+
+namespace gbsph {
+
+int fluid3d_access(gbsph_fluid3d_t h, FluidAccess* a, KParams* kp) {
+    RC(validate_params(h));
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    RC(ensure_tables(h));
+    a->pos = P4(h, 0);
+    a->vel = P4(h, 1);
+    a->force = P4(h, 2);
+    a->spos = h->spos;
+    a->svel = h->svel;
+    a->index = h->index;
+    a->keys = h->keys_c;
+    a->n = h->n;
+    a->has_hook = h->hook != nullptr;
+    a->compiled = h->compiled;
+    *kp = make_kparams(h);
+    return GBSPH_OK;
+}
+
+void fluid3d_set_record(gbsph_fluid3d_t h, float4* rec) { h->rec_force = rec; }
+
+}  // namespace gbsph
 
 extern "C" {
 

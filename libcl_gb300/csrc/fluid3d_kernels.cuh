@@ -50,6 +50,7 @@ struct KParams {
     uint32_t table_cells;
     const SceneDev* scenes;  // batches only: n_scenes entries, sorted by part/cell/brick offsets
     int n_scenes;
+    float4* rec_force;  // when set: receives each particle's force after the clip box, before the clamp
 };
 
 // Index of the scene whose range [off, next off) holds v (binary search over `n` scenes).
@@ -414,7 +415,9 @@ static __global__ void k_clip_box(const float4* __restrict__ spos, const float4*
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kp.n) return;
     const uint32_t o = index[i];
-    force[o] = clip_box_force(kp, spos[i], svel[i], force[o]);
+    const float4 f = clip_box_force(kp, spos[i], svel[i], force[o]);
+    force[o] = f;
+    if (kp.rec_force) kp.rec_force[o] = f;
 }
 
 static __global__ void k_integrate_force(float4* __restrict__ vel, const float4* __restrict__ force, KParams kp) {
@@ -444,6 +447,7 @@ static __global__ void k_post_fused(const float4* __restrict__ spos, const float
     if (i >= kp.n) return;
     const uint32_t o = index[i];
     const float4 f = clip_box_force(kp, spos[i], svel[i], force[o]);
+    if (kp.rec_force) kp.rec_force[o] = f;
     const float4 v = integrate_force(kp, vel[o], f);
     vel[o] = v;
     force[o] = kp.gravity;
@@ -714,12 +718,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                             acc = fmaf(tt * tt, tt, acc);
                             cnt += in ? 1.0f : 0.0f;
                             // branch-free append: the slot after the last real entry is
-                            // overwritten by the terminator below
+                            // overwritten by the next candidate or by the terminator below.
+                            // Once the sub-list is full, later candidates overwrite its last
+                            // entry, so a full sub-list counts as an overflow.
                             my[min(nk, sub - 1)] = (uint16_t)idx;
                             nk += (in && r2 > 0.0f) ? 1u : 0u;
                         }
                         if (nk < sub) my[nk] = NBR_END;
-                        ovf = nk > sub;
+                        ovf = nk >= sub;
                     } else {
 #pragma unroll 1
                         for (int r = 0; r < R; ++r) {
@@ -944,6 +950,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                     f.w = 0.0f;
                     if (FUSED) {
                         f = clip_box_force(kp, S.box_min, S.box_max, pi, vi, f);
+                        if (kp.rec_force) kp.rec_force[o] = f;
                         const float4 v = integrate_force(kp, v_o, f);
                         vel[o] = v;
                         force[o] = kp.gravity;

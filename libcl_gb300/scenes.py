@@ -107,6 +107,30 @@ def block_collapse_3d(nx: int = 128, ny: int = 64, nz: int = 128, seed: int = 2)
     return Scene3D(f"block_collapse_{nx}x{ny}x{nz}", pos, vel, prm)
 
 
+def differentiable_block(nx: int = 64, ny: int = 32, nz: int = 32, seed: int = 3) -> Scene3D:
+    """The differentiable-rollout scene: nx*ny*nz particles (default 65,536) on a lattice of
+    spacing 0.01 (h = 0.02) jittered by uniform +-0.05h at the lower corner of a box twice the
+    block's extent per axis (here [0,1.28]x[0,0.64]x[0,0.64], a 64x32x32 cell grid), at rest;
+    gravity -9.81 along y, rest density 1000, mass 1e-3, gas constant 3.0, viscosity 0.05,
+    dt = 5e-5 (the box, gas constant, primal viscosity and dt are choices of this generator)."""
+    h, sp = 0.02, 0.01
+    pos = lattice(nx, ny, nz, sp, (0.5 * sp, 0.5 * sp, 0.5 * sp), 0.05 * h, seed)
+    vel = np.zeros_like(pos)
+    box = 2.0 * np.array([nx, ny, nz], np.float64) * sp
+    prm = fluid_params(h, sp, 1000.0 * sp ** 3, 1000.0, 3.0, 0.05, 5e-5, (0.0, -9.81, 0.0),
+                       (0.0, 0.0, 0.0), tuple(box), tuple(int(np.ceil(b / h - 1e-9)) for b in box))
+    return Scene3D(f"differentiable_block_{nx}x{ny}x{nz}", pos, vel, prm)
+
+
+def perturbed_velocities(vel: np.ndarray, sigma: float = 0.1, seed: int = 6) -> np.ndarray:
+    """vel + N(0, sigma^2) per component (x, y, z), float32 [N, 4]: the target run's initial
+    velocities of the differentiable rollout."""
+    out = vel.copy()
+    n = vel.shape[0]
+    out[:, :3] += (SplitMix64(seed).normal(3 * n).reshape(n, 3) * sigma).astype(np.float32)
+    return out
+
+
 def dam_break_2d(nx: int = 128, ny: int = 128, seed: int = 1) -> Scene3D:
     """2D dam break: 128x128 particles (spacing 0.5h, h = 0.01) jittered +-0.05h, anchored at
     the lower-left corner of a [0,1]x[0,1] box; gravity -9.81, rest density 1000, gas constant

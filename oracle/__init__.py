@@ -59,6 +59,9 @@ def lib() -> C.CDLL:
             "orc2d_compute_border": (None, [P, C.c_int, C.c_int, P, P, P]),
             "orc2d_step": (None, [P, U, P, P, P, C.c_int, C.c_int, P, P, P, P, P, P, P, P]),
             "orc_set_num_threads": (None, [C.c_int]),
+            "orc_run_f64": (C.c_int, [P, P, P, U, P, U]),
+            "orc_adjoint_f64": (C.c_int, [P, P, P, U, P, U, U, P, P, P, P, P]),
+            "orc_adjoint_states_f64": (C.c_int, [P, P, P, U, P, U, P, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -242,3 +245,37 @@ def step_2d(state: np.ndarray, p, border_state: np.ndarray, border_vec: np.ndarr
     lib().orc2d_step(_p(state), n, _pp(p), _p(border_state), _p(border_vec), w, h, _p(r.cell), _p(r.index),
                      _p(r.sorted), _p(r.pstate), _p(r.relaxed), _p(r.prev), _p(r.cell_start), _p(r.cell_end))
     return r
+
+
+def run_f64(pos64: np.ndarray, vel64: np.ndarray, force64: np.ndarray, params, steps: int) -> None:
+    """`steps` FP64 steps in place (keys from the positions rounded to FP32)."""
+    rc = lib().orc_run_f64(_p(pos64), _p(vel64), _p(force64), pos64.shape[0], _pp(params), steps)
+    assert rc == 0, rc
+
+
+def adjoint_f64(pos0, vel0, force0, params, steps: int, every: int, gpos, gvel=None):
+    """FP64 adjoint of `steps` steps (LINEAR_GRID, 3D): returns (dL/dpos0, dL/dvel0,
+    dL/dstiffness, dL/dviscosity) for the final-state gradients gpos, gvel (float64 [N, 4])."""
+    n = pos0.shape[0]
+    gp0 = np.empty((n, 4), np.float64)
+    gv0 = np.empty((n, 4), np.float64)
+    gpar = np.empty(2, np.float64)
+    rc = lib().orc_adjoint_f64(_p(pos0), _p(vel0), _p(force0), n, _pp(params), steps, every, _p(gpos),
+                               None if gvel is None else _p(gvel), _p(gp0), _p(gv0), _p(gpar))
+    assert rc == 0, rc
+    return gp0, gv0, float(gpar[0]), float(gpar[1])
+
+
+def adjoint_states_f64(states_pos, states_vel, force0, params, gpos, gvel=None):
+    """FP64 adjoint along a given trajectory: states_pos / states_vel float32 [steps, N, 4]
+    (the state before each step), force0 float64 [N, 4]. Returns like adjoint_f64."""
+    steps, n = states_pos.shape[:2]
+    sp = np.ascontiguousarray(states_pos, np.float32)
+    sv = np.ascontiguousarray(states_vel, np.float32)
+    gp0 = np.empty((n, 4), np.float64)
+    gv0 = np.empty((n, 4), np.float64)
+    gpar = np.empty(2, np.float64)
+    rc = lib().orc_adjoint_states_f64(_p(sp), _p(sv), _p(force0), n, _pp(params), steps, _p(gpos),
+                                      None if gvel is None else _p(gvel), _p(gp0), _p(gv0), _p(gpar))
+    assert rc == 0, rc
+    return gp0, gv0, float(gpar[0]), float(gpar[1])

@@ -502,10 +502,11 @@ void to_t(const float* src, T* dst, size_t count) {
 // pos/vel/force are in/out float4[n]; the FP32 positions `fpos_key` (same as pos for T=float)
 // give the keys. Outputs the sorted keys, index, sorted pos/vel (w = density / pressure) and
 // the cell tables. `ref_sort` selects the restated reference sort (else std::stable_sort).
+// If `fwall` is set it receives the force after the clip box (particle order).
 template <class T>
 int step_t(T* pos, T* vel, T* force, const float* fpos_key, uint32_t n,
            const gbsph_fluid3d_params& P, uint32_t* cell, uint32_t* index, T* spos, T* svel,
-           uint32_t* cellStart, uint32_t* cellEnd, int ref_sort) {
+           uint32_t* cellStart, uint32_t* cellEnd, int ref_sort, T* fwall = nullptr) {
     orc_hash(fpos_key, n, &P, cell, index);
     int rc = ref_sort ? orc_radix_sort_reference(cell, index, n, n, 0, 24)
                       : orc_stable_sort(cell, index, n, 0, 24);
@@ -525,6 +526,7 @@ int step_t(T* pos, T* vel, T* force, const float* fpos_key, uint32_t n,
     density_t<T>(spos, svel, fs.data(), cellStart, cellEnd, n, P);
     forces_t<T>(spos, svel, force, index, fs.data(), cellStart, cellEnd, n, P);
     clip_box_t<T>(spos, svel, force, index, n, P);
+    if (fwall) std::memcpy(fwall, force, 4 * sizeof(T) * (size_t)n);
     integrate_force_t<T>(vel, force, n, P);
     gravity_t<T>(force, n, P);
     integrate_velocity_t<T>(pos, vel, n, P);
@@ -600,6 +602,284 @@ void orc_set_num_threads(int n) {
 #else
     (void)n;
 #endif
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// FP64 adjoint of the LINEAR_GRID step (hand-derived reverse of clCalculateDensity,
+// clCalculateForces, clClipBox, clIntegrateForce and clIntegrateVelocity,
+// libCL/phys/oclFluid3D.cl:150-298,304-361), with each step's permutation and neighbour
+// sets held fixed. Per step, in sorted order i with particle o = index[i], d = x_i - x_j,
+// r = |d|, D = 1/(rho_i rho_j), w = m dL/dF:
+//   integration:  dL/dv += dt dL/dx';  dL/dF = dt dL/dv (through the clamp's Jacobian when
+//                 |F| exceeded the limit); active walls add -2000 dL/dF_a to dL/dx_a and
+//                 -256 dL/dF_a to dL/dv_a
+//   forces:       per pair, with dw = w_i - w_j, phi = (h-r)^2/r, dv = v_j - v_i:
+//                 dL/dx_i += Cp (p_i+p_j) D (phi dw + phi'(r)/r (d.dw) d) - Cv D (dw.dv)/r d
+//                 dL/dv_i -= Cv D (h-r) dw
+//                 dL/dp_i += Cp D phi (d.dw)
+//                 dL/drho_i -= D/rho_i (Cp (p_i+p_j) phi (d.dw) + Cv (h-r) (dw.dv))
+//   pressure law: dL/dS_i = m K (dL/drho_i + k dL/dp_i) where rho = m K S (else 0),
+//                 dL/dk += (rho_i - rho0) dL/dp_i, dL/dmu += 45/(pi h^6) w_i . sum_j D (h-r) dv
+//   density:      dL/dx_i += -6 sum_j (h^2 - r^2)^2 (dL/dS_i + dL/dS_j) d
+// Each pair's terms depend on i and j symmetrically, so every sum gathers over i's own
+// neighbours (the same loops as the forward kernels).
+// ---------------------------------------------------------------------------------------
+namespace {
+
+struct TapeF64 {
+    std::vector<uint32_t> cell, index, cs, ce;
+    std::vector<double> spos, svel, fwall;
+    std::vector<float> fs;  // FP32 sorted positions: the cell lookups
+};
+
+void record_step_f64(double* pos, double* vel, double* force, uint32_t n, const gbsph_fluid3d_params& P,
+                     TapeF64& t) {
+    const size_t cells = table_size(P);
+    t.cell.resize(n);
+    t.index.resize(n);
+    t.cs.resize(cells);
+    t.ce.resize(cells);
+    t.spos.resize(4 * (size_t)n);
+    t.svel.resize(4 * (size_t)n);
+    t.fwall.resize(4 * (size_t)n);
+    std::vector<float> fpos(4 * (size_t)n);
+    for (size_t i = 0; i < 4 * (size_t)n; i++) fpos[i] = (float)pos[i];
+    step_t<double>(pos, vel, force, fpos.data(), n, P, t.cell.data(), t.index.data(), t.spos.data(),
+                   t.svel.data(), t.cs.data(), t.ce.data(), 0, t.fwall.data());
+    t.fs.resize(4 * (size_t)n);
+    for (size_t i = 0; i < n; i++) std::memcpy(&t.fs[4 * i], &fpos[4 * (size_t)t.index[i]], 16);
+}
+
+// Calls f(j, dx, dy, dz, r) for every neighbour j != i with r < h (FP64 distances, cells
+// from the FP32 positions), as the forward loops of density_t / forces_t visit them.
+template <class F>
+void for_neighbours_f64(const TapeF64& t, const gbsph_fluid3d_params& P, int64_t i, F&& f) {
+    const double h = P.cellSize;
+    int g[3];
+    grid_position(P, t.fs[4 * i], t.fs[4 * i + 1], t.fs[4 * i + 2], g);
+    uint32_t cells[27];
+    const int nc = neighbour_cells(P, g, cells);
+    const double* xi = &t.spos[4 * i];
+    for (int c = 0; c < nc; c++) {
+        const uint32_t start = t.cs[cells[c]];
+        if (start == kEmpty) continue;
+        const uint32_t end = t.ce[cells[c]];
+        for (uint32_t j = start; j < end; j++) {
+            if (j == (uint32_t)i) continue;
+            const double* xj = &t.spos[4 * (size_t)j];
+            const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+            const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+            if (r < h) f(j, dx, dy, dz, r);
+        }
+    }
+}
+
+// One step backwards: gx/gv (particle order) hold dL/d(state after the step) on entry and
+// dL/d(state before the step) on return; acc_k / acc_mu (particle order) accumulate.
+void adjoint_step_f64(const TapeF64& t, uint32_t n, const gbsph_fluid3d_params& P, double* gx, double* gv,
+                      double* acc_k, double* acc_mu) {
+    const double dt = P.deltaTime, h = P.cellSize, m = P.mass, cp = P.pressureConstant, cv = P.viscosityConstant;
+    const double mK = (double)P.mass * (double)P.kernelConstant, k = P.stiffness, rho0 = P.density;
+    const double pi = (double)(float)M_PI;
+    const double c45 = 45.0 / (pi * std::pow((double)P.cellSize, 6.0));
+    std::vector<double> w(3 * (size_t)n), gxs(3 * (size_t)n), gvs(3 * (size_t)n), gS(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const size_t o = t.index[i];
+        const double* x = &t.spos[4 * i];
+        const double* f = &t.fwall[4 * o];
+        double gvt[3], gf[3];
+        for (int a = 0; a < 3; a++) {
+            gvt[a] = gv[4 * o + a] + dt * gx[4 * o + a];
+            gf[a] = dt * gvt[a];
+        }
+        const double f2 = f[0] * f[0] + f[1] * f[1] + f[2] * f[2] + f[3] * f[3];
+        const double speed = std::sqrt(f2);
+        if (speed > (double)P.velocitylimit) {
+            const double s = (double)P.velocitylimit / speed, fg = (f[0] * gf[0] + f[1] * gf[1] + f[2] * gf[2]) / f2;
+            for (int a = 0; a < 3; a++) gf[a] = s * (gf[a] - f[a] * fg);
+        }
+        double ax[3] = {0, 0, 0}, av[3] = {0, 0, 0};
+        const double r = P.particleRadius, eps = (double)0.00001f;
+        auto wall = [&](int a, double diff) {
+            if (diff > eps) {
+                ax[a] -= 2000.0 * gf[a];
+                av[a] -= 256.0 * gf[a];
+            }
+        };
+        wall(1, r - (x[1] - (double)P.boxMin[1]));
+        wall(1, r - ((double)P.boxMax[1] - x[1]));
+        wall(2, r - (x[2] - (double)P.boxMin[2]));
+        wall(2, r - ((double)P.boxMax[2] - x[2]));
+        wall(0, r - (x[0] - (double)P.boxMin[0]));
+        wall(0, r - ((double)P.boxMax[0] - x[0]));
+        for (int a = 0; a < 3; a++) {
+            w[3 * i + a] = m * gf[a];
+            gxs[3 * i + a] = gx[4 * o + a] + ax[a];
+            gvs[3 * i + a] = gvt[a] + av[a];
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const double* xi = &t.spos[4 * i];
+        const double* vi = &t.svel[4 * i];
+        const double* wi = &w[3 * i];
+        const double rho_i = xi[3], p_i = vi[3];
+        double ax[3] = {0, 0, 0}, av[3] = {0, 0, 0}, b[3] = {0, 0, 0}, ap = 0, arho = 0;
+        int count = 0;
+        for_neighbours_f64(t, P, i, [&](uint32_t j, double dx, double dy, double dz, double r) {
+            count++;
+            if (!(r > 0)) return;
+            const double* xj = &t.spos[4 * (size_t)j];
+            const double* vj = &t.svel[4 * (size_t)j];
+            const double* wj = &w[3 * (size_t)j];
+            const double hr = h - r, D = 1.0 / (rho_i * xj[3]), Pp = p_i + vj[3];
+            const double phi = hr * hr / r, dphi_r = -hr * (h + r) / (r * r * r);
+            const double d[3] = {dx, dy, dz};
+            const double dw[3] = {wi[0] - wj[0], wi[1] - wj[1], wi[2] - wj[2]};
+            const double dv[3] = {vj[0] - vi[0], vj[1] - vi[1], vj[2] - vi[2]};
+            const double ddw = d[0] * dw[0] + d[1] * dw[1] + d[2] * dw[2];
+            const double dwdv = dw[0] * dv[0] + dw[1] * dv[1] + dw[2] * dv[2];
+            for (int a = 0; a < 3; a++) {
+                ax[a] += cp * Pp * D * (phi * dw[a] + dphi_r * ddw * d[a]) - cv * D * dwdv / r * d[a];
+                av[a] -= cv * D * hr * dw[a];
+                b[a] += D * hr * dv[a];
+            }
+            ap += cp * D * phi * ddw;
+            arho -= D / rho_i * (cp * Pp * phi * ddw + cv * hr * dwdv);
+        });
+        for (int a = 0; a < 3; a++) {
+            gxs[3 * i + a] += ax[a];
+            gvs[3 * i + a] += av[a];
+        }
+        gS[i] = (count > 2 && rho_i > 1.0) ? mK * (arho + k * ap) : 0.0;
+        const size_t o = t.index[i];
+        acc_k[o] += (rho_i - rho0) * ap;
+        acc_mu[o] += c45 * (wi[0] * b[0] + wi[1] * b[1] + wi[2] * b[2]);
+    }
+    const double h2 = h * h;
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        double a[3] = {0, 0, 0};
+        for_neighbours_f64(t, P, i, [&](uint32_t j, double dx, double dy, double dz, double r) {
+            const double tt = h2 - r * r;
+            const double c = -6.0 * tt * tt * (gS[i] + gS[j]);
+            a[0] += c * dx;
+            a[1] += c * dy;
+            a[2] += c * dz;
+        });
+        const size_t o = t.index[i];
+        for (int q = 0; q < 3; q++) {
+            gx[4 * o + q] = gxs[3 * i + q] + a[q];
+            gv[4 * o + q] = gvs[3 * i + q];
+        }
+        gx[4 * o + 3] = 0;
+        gv[4 * o + 3] = 0;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+// `steps` FP64 steps in place (keys from the positions rounded to FP32 before each step).
+int orc_run_f64(double* pos, double* vel, double* force, uint32_t n, const gbsph_fluid3d_params* P,
+                uint32_t steps) {
+    TapeF64 t;
+    for (uint32_t s = 0; s < steps; s++) record_step_f64(pos, vel, force, n, *P, t);
+    return 0;
+}
+
+// Reverse-mode gradients of a loss on the state after `steps` FP64 steps from (pos0, vel0,
+// force0): given dL/dpos, dL/dvel of the final state (float4-strided doubles; gvel may be
+// NULL), writes dL/dpos0, dL/dvel0 and gparams[0] = dL/dstiffness, gparams[1] =
+// dL/dviscosity. Checkpoints every `every` steps and recomputes each segment.
+int orc_adjoint_f64(const double* pos0, const double* vel0, const double* force0, uint32_t n,
+                    const gbsph_fluid3d_params* P, uint32_t steps, uint32_t every, const double* gpos,
+                    const double* gvel, double* gpos0, double* gvel0, double* gparams) {
+    if (P->keyMode != GBSPH_KEY_LINEAR_GRID || P->dims != 3 || every == 0) return -1;
+    const size_t N4 = 4 * (size_t)n;
+    const uint32_t nseg = (steps + every - 1) / every;
+    std::vector<std::vector<double>> ck(nseg, std::vector<double>(3 * N4));
+    std::vector<double> pos(pos0, pos0 + N4), vel(vel0, vel0 + N4), force(force0, force0 + N4);
+    TapeF64 scratch;
+    for (uint32_t s = 0; s < steps; s++) {
+        if (s % every == 0) {
+            std::vector<double>& c = ck[s / every];
+            std::memcpy(c.data(), pos.data(), N4 * 8);
+            std::memcpy(c.data() + N4, vel.data(), N4 * 8);
+            std::memcpy(c.data() + 2 * N4, force.data(), N4 * 8);
+        }
+        record_step_f64(pos.data(), vel.data(), force.data(), n, *P, scratch);
+    }
+    std::vector<double> gx(gpos, gpos + N4), gv(N4, 0.0), acc_k(n, 0.0), acc_mu(n, 0.0);
+    if (gvel) std::memcpy(gv.data(), gvel, N4 * 8);
+    std::vector<TapeF64> tape(every);
+    for (uint32_t seg = nseg; seg-- > 0;) {
+        const uint32_t s0 = seg * every, s1 = std::min(steps, s0 + every);
+        const std::vector<double>& c = ck[seg];
+        std::memcpy(pos.data(), c.data(), N4 * 8);
+        std::memcpy(vel.data(), c.data() + N4, N4 * 8);
+        std::memcpy(force.data(), c.data() + 2 * N4, N4 * 8);
+        for (uint32_t s = s0; s < s1; s++) record_step_f64(pos.data(), vel.data(), force.data(), n, *P, tape[s - s0]);
+        for (uint32_t s = s1; s-- > s0;) adjoint_step_f64(tape[s - s0], n, *P, gx.data(), gv.data(), acc_k.data(), acc_mu.data());
+    }
+    if (gpos0) std::memcpy(gpos0, gx.data(), N4 * 8);
+    if (gvel0) std::memcpy(gvel0, gv.data(), N4 * 8);
+    if (gparams) {
+        double a = 0, b = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            a += acc_k[i];
+            b += acc_mu[i];
+        }
+        gparams[0] = a;
+        gparams[1] = b;
+    }
+    return 0;
+}
+
+// The FP64 adjoint along a given trajectory: states_pos / states_vel hold the float4 state
+// before each of the `steps` steps (step-major, float32, e.g. read back from the GPU after
+// every step); force0 is the force buffer before the first step (later steps start from the
+// gravity vector, as the step leaves it). Each step is re-linearised in FP64 around the given
+// state, so branch decisions and neighbour sets follow that trajectory.
+int orc_adjoint_states_f64(const float* states_pos, const float* states_vel, const double* force0, uint32_t n,
+                           const gbsph_fluid3d_params* P, uint32_t steps, const double* gpos, const double* gvel,
+                           double* gpos0, double* gvel0, double* gparams) {
+    if (P->keyMode != GBSPH_KEY_LINEAR_GRID || P->dims != 3) return -1;
+    const size_t N4 = 4 * (size_t)n;
+    std::vector<double> gx(gpos, gpos + N4), gv(N4, 0.0), acc_k(n, 0.0), acc_mu(n, 0.0);
+    if (gvel) std::memcpy(gv.data(), gvel, N4 * 8);
+    std::vector<double> pos(N4), vel(N4), force(N4);
+    TapeF64 t;
+    for (uint32_t s = steps; s-- > 0;) {
+        for (size_t i = 0; i < N4; i++) {
+            pos[i] = states_pos[s * N4 + i];
+            vel[i] = states_vel[s * N4 + i];
+        }
+        if (s == 0) {
+            std::memcpy(force.data(), force0, N4 * 8);
+        } else {
+            for (size_t i = 0; i < n; i++)
+                for (int c = 0; c < 4; c++) force[4 * i + c] = P->gravity[c];
+        }
+        record_step_f64(pos.data(), vel.data(), force.data(), n, *P, t);
+        adjoint_step_f64(t, n, *P, gx.data(), gv.data(), acc_k.data(), acc_mu.data());
+    }
+    if (gpos0) std::memcpy(gpos0, gx.data(), N4 * 8);
+    if (gvel0) std::memcpy(gvel0, gv.data(), N4 * 8);
+    if (gparams) {
+        double a = 0, b = 0;
+        for (uint32_t i = 0; i < n; i++) {
+            a += acc_k[i];
+            b += acc_mu[i];
+        }
+        gparams[0] = a;
+        gparams[1] = b;
+    }
+    return 0;
 }
 
 }  // extern "C"

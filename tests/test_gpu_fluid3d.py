@@ -308,3 +308,29 @@ def test_dense_clump_takes_the_fallback_paths(cuda):
     errs = compare_fast(g, gs, r, rs, sc.pos, tol=1e-3)
     print("clump errors:", errs)
     assert f.sync_status() == OK
+
+
+def test_dense_cloud_force_change_within_tolerance(cuda):
+    """A uniform random cloud at about 15 particles per cell: the lanes' neighbour sub-lists
+    of the density kernel are often exactly full, the case where a list entry could be
+    overwritten by a later out-of-range candidate. The velocity change of one step (force *
+    dt, without the initial velocities that would hide a force error) must agree with the
+    restatement within 1e-3."""
+    from libcl_gb300.scenes import SplitMix64
+    sc = block_collapse_3d(8, 8, 8)
+    nxc, nyc, nzc = 20, 10, 20
+    n = 15 * nxc * nyc * nzc
+    rng = SplitMix64(123)
+    pos = np.zeros((n, 4), np.float32)
+    pos[:, :3] = (rng.uniform(3 * n).reshape(n, 3) * np.array([nxc, nyc, nzc]) * 0.02 + 0.04).astype(np.float32)
+    sc.pos = pos
+    sc.vel = np.zeros_like(pos)
+    vel = perturbed(sc, sigma=0.05)
+    f = make_fluid(sc, fused=True, vel=vel)
+    f.compute()
+    gs = state(f)
+    r, rs = oracle_step(sc, vel)
+    e = rel_err(gs["vel"] - vel, rs["vel"] - vel)
+    print("velocity-change relative error:", e)
+    assert e <= 1e-3, e
+    assert f.sync_status() == OK
