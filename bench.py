@@ -391,6 +391,7 @@ def main(argv=None) -> int:
     import torch.distributed as dist
     from libcl_gb300 import OPT_PROFILE, Fluid3D
     from libcl_gb300.scenes import block_collapse_3d
+    from libcl_gb300.sharding import max_over_ranks
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -425,10 +426,7 @@ def main(argv=None) -> int:
         dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     t_ms = float(sum(step_ms))
-    if world > 1:
-        t = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
+    t_ms = max_over_ranks(t_ms, device="cuda")
     status = fluid.sync_status()
     if status != 0:
         print(f"device status {status}: {fluid.last_error()}", file=sys.stderr)
