@@ -484,6 +484,9 @@ __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, u
     constexpr int R = DIMS == 3 ? 9 : 3;
     const int W = kp.bw;
     const int t = threadIdx.x;
+    // a single scene's grid comes from kp (no barrier needed); a batch's from its scene
+    // table, through shared memory. The barrier after the table loads publishes S's scene
+    // fields before any warp reads them.
     if (t == 0) {
         if (BATCH) {
             const int sc = scene_of<2>(kp.scenes, kp.n_scenes, bid);
@@ -511,16 +514,17 @@ __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, u
             S.lbrick = bid;
         }
     }
-    __syncthreads();
-    const uint32_t lb = S.lbrick;
-    const int nx = S.nx, ny = S.ny, nz = S.nz;
-    const int bx = (int)(lb % (uint32_t)S.bxn);
-    const uint32_t yz = lb / (uint32_t)S.bxn;
+    if (BATCH) __syncthreads();
+    const uint32_t lb = BATCH ? S.lbrick : bid;
+    const int nx = BATCH ? S.nx : kp.nx, ny = BATCH ? S.ny : kp.ny, nz = BATCH ? S.nz : kp.nz;
+    const uint32_t bxn = BATCH ? (uint32_t)S.bxn : (uint32_t)kp.bxn;
+    const int bx = (int)(lb % bxn);
+    const uint32_t yz = lb / bxn;
     const int y = (int)(yz % (uint32_t)ny);
     const int z = (int)(yz / (uint32_t)ny);
     x0 = bx * W;
     ncell = min(W, nx - x0);
-    const uint2* tab = table + S.cell_off;
+    const uint2* tab = BATCH ? table + S.cell_off : table;
     for (int idx = t; idx < R * (W + 2); idx += BRICK_THREADS) {
         const int r = idx / (W + 2), c = idx - r * (W + 2);
         const int cy = y + (r % 3) - 1;
@@ -620,11 +624,12 @@ constexpr uint32_t NBR_CAP = 64;         // neighbour slots per particle (uint16
 constexpr uint16_t NBR_END = 0xFFFFu;    // terminates a lane's neighbour sub-list
 constexpr uint32_t WLIST_STRIDE = NBR_CAP + 2;  // shared-memory stride per target (33 words: no bank conflicts)
 constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists the force kernel stages
+constexpr uint32_t GROUP_MAX = 16;              // targets a warp takes at once (both passes)
 
 
 // Dynamic shared memory of the brick kernels.
 constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * CELL_LIST_MAX * 2 +
-                                (size_t)BRICK_WARPS * 32 * WLIST_STRIDE * 2;
+                                (size_t)BRICK_WARPS * GROUP_MAX * WLIST_STRIDE * 2;
 constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
 
 // Slots of each lane's sub-list when Q lanes share a target: a multiple of 8 (one 16-byte
@@ -640,8 +645,9 @@ __device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
 // lists the cell's candidates (the 3 cells of each neighbour row, in row order) as staged
 // indices, then lanes (target, stride q) walk that list. Every target also meets itself
 // (r^2 = 0, term h^6, count 1); that term is removed after the sum instead of testing the
-// index of every candidate. Each lane records its in-range neighbours (r^2 > 0) as staged
-// indices in its own sub-list of nbr[gi][NBR_CAP] (in candidate order, NBR_END-terminated);
+// index of every candidate. Each lane records its in-range candidates (the target itself
+// included) as staged indices in its own sub-list of nbr[gi][NBR_CAP] (in candidate order,
+// NBR_END-terminated); the lists' lengths are the counts the reference's count > 2 test uses;
 // nbr_flag[gi] = 1 when a sub-list overflowed or the brick could not be staged.
 template <int DIMS, bool BATCH>
 __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
@@ -657,7 +663,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
     __shared__ BrickShared S;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint16_t* clist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * CELL_LIST_MAX;
-    uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + BRICK_WARPS * CELL_LIST_MAX + warp * 32 * WLIST_STRIDE;
+    uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + BRICK_WARPS * CELL_LIST_MAX + warp * GROUP_MAX * WLIST_STRIDE;
     if (t == 0) {
         mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
         fence_mbar_init();
@@ -667,11 +673,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
     const uint32_t n_bricks = counters[0];
     const float h2 = kp.h2, thr = kp.r2_thresh;
     const uint32_t lt = lanemask_lt();
+    // the next brick's id is fetched while this one is processed
+    if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
     for (;;) {
-        if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
         __syncthreads();
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
+        uint32_t next_brick = 0;
+        if (t == 0) next_brick = atomicAdd(&counters[1], 1u);
         int x0, ncell;
         brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         const bool staged = brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr);
@@ -689,8 +698,8 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                 __syncwarp();
             }
             const bool flat = staged && T <= CELL_LIST_MAX;
-            for (uint32_t g0 = 0; g0 < nt; g0 += 32) {
-                const uint32_t tg = min(32u, nt - g0), Q = 32u / tg;
+            for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
+                const uint32_t tg = min(GROUP_MAX, nt - g0), Q = 32u / tg;
                 const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
                 const bool active = q < Q;
                 const uint32_t tl = t0 + g0 + ti;
@@ -698,11 +707,11 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                 const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
                 const uint32_t sub = nbr_sub(Q);
                 uint16_t* my = wlist + ti * WLIST_STRIDE + q * sub;
-                float acc = 0.0f, cnt = 0.0f;
+                float acc = 0.0f;
+                uint32_t nk = 0;  // in-range candidates of this lane (the target itself included)
                 bool ovf = !flat;
                 if (active) {
                     if (flat) {
-                        uint32_t nk = 0;
 #pragma unroll 4
                         for (uint32_t k = q; k < T; k += Q) {
                             const uint32_t idx = clist[k];
@@ -716,13 +725,13 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                             const bool in = r2 < thr;
                             const float tt = in ? h2 - r2 : 0.0f;
                             acc = fmaf(tt * tt, tt, acc);
-                            cnt += in ? 1.0f : 0.0f;
                             // branch-free append: the slot after the last real entry is
                             // overwritten by the next candidate or by the terminator below.
                             // Once the sub-list is full, later candidates overwrite its last
-                            // entry, so a full sub-list counts as an overflow.
+                            // entry, so a full sub-list counts as an overflow. The target and
+                            // coincident particles (r^2 = 0) are listed; the force pass skips them.
                             my[min(nk, sub - 1)] = (uint16_t)idx;
-                            nk += (in && r2 > 0.0f) ? 1u : 0u;
+                            nk += in ? 1u : 0u;
                         }
                         if (nk < sub) my[nk] = NBR_END;
                         ovf = nk >= sub;
@@ -742,13 +751,13 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                                 const bool in = r2 < thr;
                                 const float tt = in ? h2 - r2 : 0.0f;
                                 acc = fmaf(tt * tt, tt, acc);
-                                cnt += in ? 1.0f : 0.0f;
+                                nk += in ? 1u : 0u;
                             }
                         }
                     }
                 }
                 acc = reduce_q(acc, q, Q, tg);
-                cnt = reduce_q(cnt, q, Q, tg);
+                float cnt = reduce_q((float)nk, q, Q, tg);
                 uint32_t gm = 0;  // lanes sharing this lane's target
                 for (uint32_t k = 0; k < Q; ++k) gm |= 1u << (ti + k * tg);
                 const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & gm;
@@ -777,6 +786,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
             }
             __syncwarp();  // clist is rebuilt for the warp's next cell
         }
+        if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
 }
 
@@ -792,6 +802,29 @@ __device__ __forceinline__ void force_pair(const float4& pi, const float4& vi, f
     const float hr = h - vlen;
     const float dd = inv_rho_i * __frcp_rn(pj.w);  // 1 / (rho_i rho_j)
     const float sp = (vi.w + vj.w) * dd * hr * hr * inv;
+    acc[0] = fmaf(sp, dx, acc[0]);
+    acc[1] = fmaf(sp, dy, acc[1]);
+    acc[2] = fmaf(sp, dz, acc[2]);
+    const float cv = hr * dd;
+    acc[3] = fmaf(vj.x - vi.x, cv, acc[3]);
+    acc[4] = fmaf(vj.y - vi.y, cv, acc[4]);
+    acc[5] = fmaf(vj.z - vi.z, cv, acc[5]);
+}
+
+// force_pair on the force pass's staged copies, whose w lanes hold a = 1/rho (positions) and
+// b = p/rho (velocities): (p_i + p_j) / (rho_i rho_j) = b_i a_j + a_i b_j. Skips r = 0 (the
+// target itself, which its list holds, and coincident particles).
+template <int DIMS>
+__device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& vi, const float4& pj,
+                                               const float4& vj, float h, float* acc) {
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = DIMS == 3 ? pi.z - pj.z : 0.0f;
+    float r2 = fmaf(dy, dy, dx * dx);
+    if (DIMS == 3) r2 = fmaf(dz, dz, r2);
+    if (!(r2 > 0.0f)) return;
+    const float inv = rsqrtf(r2);
+    const float hr = h - r2 * inv;
+    const float dd = pi.w * pj.w;  // 1 / (rho_i rho_j)
+    const float sp = fmaf(vi.w, pj.w, pi.w * vj.w) * (hr * hr * inv);
     acc[0] = fmaf(sp, dx, acc[0]);
     acc[1] = fmaf(sp, dy, acc[1]);
     acc[2] = fmaf(sp, dz, acc[2]);
@@ -837,11 +870,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
     const float4* s_pos = s_buf;
     const float4* s_vel = s_buf + BRICK_CAP;
     uint16_t* s_lists = reinterpret_cast<uint16_t*>(s_buf + 2 * BRICK_CAP);
+    // the next brick's id is fetched while this one is processed
+    if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
     for (;;) {
-        if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
         __syncthreads();
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
+        uint32_t next_brick = 0;
+        if (t == 0) next_brick = atomicAdd(&counters[2], 1u);
         int x0, ncell;
         brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         // the brick's targets are consecutive particles: stage their lists with the rows
@@ -869,18 +905,29 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
         }
         __syncthreads();
         const bool staged = S.total <= BRICK_CAP && S.total > 0;
-        if (staged && !brick_wait(S, phase, err)) return;
+        if (staged) {
+            if (!brick_wait(S, phase, err)) return;
+            // w lanes of the staged copies: 1/rho and p/rho (force_pair_pre)
+            for (uint32_t k = t; k < S.total; k += BRICK_THREADS) {
+                const float a = __frcp_rn(s_buf[k].w);
+                s_buf[k].w = a;
+                s_buf[BRICK_CAP + k].w *= a;
+            }
+            __syncthreads();
+        }
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
-            for (uint32_t g0 = 0; g0 < nt; g0 += 32) {
-                const uint32_t tg = min(32u, nt - g0), Q = 32u / tg;
+            // the same target groups as the density pass: its lists are split into sub-lists
+            // by the group's lane count
+            for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
+                const uint32_t tg = min(GROUP_MAX, nt - g0), Q = 32u / tg;
                 const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
                 const bool active = q < Q;
                 const uint32_t tl = t0 + g0 + ti;
                 const uint32_t gi = S.lo[RC] + tl;
                 const float4 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
                 const float4 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
-                const float inv_rho_i = 1.0f / pi.w;
+                const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
                 float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
                 // prefetch what the integration needs so its latency overlaps the pair loop
                 uint32_t o = 0;
@@ -918,7 +965,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                                 done = true;
                                 break;
                             }
-                            force_pair<DIMS>(pi, vi, inv_rho_i, s_pos[idx], s_vel[idx], kp.h, acc);
+                            force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
                         }
                     }
                 } else if (active) {
@@ -935,7 +982,10 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                                 const float dz = pi.z - pj.z;
                                 r2 = fmaf(dz, dz, r2);
                             }
-                            if (r2 < kp.r2_thresh && r2 > 0.0f) force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
+                            if (r2 < kp.r2_thresh && r2 > 0.0f) {
+                                if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
+                                else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
+                            }
                         }
                     }
                 }
@@ -961,6 +1011,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                 }
             }
         }
+        if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
 }
 
