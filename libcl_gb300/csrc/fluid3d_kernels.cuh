@@ -619,17 +619,15 @@ __device__ __forceinline__ float reduce_q(float v, uint32_t q, uint32_t Q, uint3
 // stage (or fall back for) exactly the same bricks: the neighbour lists the density kernel
 // records are indices into that staging.
 constexpr uint32_t BRICK_CAP = 1536;
-constexpr uint32_t CELL_LIST_MAX = 512;  // candidates of one target cell, per warp (uint16)
 constexpr uint32_t NBR_CAP = 64;         // neighbour slots per particle (uint16), split over the Q lanes
 constexpr uint16_t NBR_END = 0xFFFFu;    // terminates a lane's neighbour sub-list
-constexpr uint32_t WLIST_STRIDE = NBR_CAP + 2;  // shared-memory stride per target (33 words: no bank conflicts)
+constexpr uint32_t WLIST_STRIDE = NBR_CAP + 8;  // shared-memory stride per target (halves; 16-byte rows)
 constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists the force kernel stages
 constexpr uint32_t GROUP_MAX = 16;              // targets a warp takes at once (both passes)
 
 
 // Dynamic shared memory of the brick kernels.
-constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * CELL_LIST_MAX * 2 +
-                                (size_t)BRICK_WARPS * GROUP_MAX * WLIST_STRIDE * 2;
+constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * GROUP_MAX * WLIST_STRIDE * 2;
 constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
 
 // Slots of each lane's sub-list when Q lanes share a target: a multiple of 8 (one 16-byte
@@ -639,16 +637,47 @@ __device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
     return s >= 8 ? (s & ~7u) : (s >= 4 ? 4u : 2u);
 }
 
+// Lane layout of a group of tg targets (1 <= tg <= GROUP_MAX) on a warp: lane = q * tg + ti
+// serves target ti with stride q of Q = 32 / tg (lanes with q >= Q idle). tq packs ti | q << 8;
+// info packs Q | nbr_sub(Q) << 8; group << ti is the mask of the lanes serving target ti.
+// Both neighbour passes use it, so the density pass's sub-lists are the force pass's.
+struct LaneMap {
+    uint16_t tq[GROUP_MAX + 1][32];
+    uint32_t info[GROUP_MAX + 1];
+    uint32_t group[GROUP_MAX + 1];
+};
+
+__device__ __forceinline__ void lane_map_init(LaneMap& L) {
+    for (uint32_t i = threadIdx.x; i < (GROUP_MAX + 1) * 32; i += blockDim.x) {
+        const uint32_t tg = i / 32, lane = i % 32;
+        if (tg == 0) {
+            L.tq[0][lane] = 0;
+            if (lane == 0) L.info[0] = L.group[0] = 0;
+            continue;
+        }
+        const uint32_t Q = 32 / tg;
+        L.tq[tg][lane] = (uint16_t)((lane % tg) | ((lane / tg) << 8));
+        if (lane == 0) {
+            uint32_t m = 0;
+            for (uint32_t k = 0; k < Q; ++k) m |= 1u << (k * tg);
+            L.info[tg] = Q | (nbr_sub(Q) << 8);
+            L.group[tg] = m;
+        }
+    }
+}
+
 // Density + pressure for every particle of the occupied bricks (persistent CTAs).
 // Writes sorted position .w = density and sorted velocity .w = pressure, as
-// clCalculateDensity does (libCL/phys/oclFluid3D.cl:189-199). Per target cell, a warp first
-// lists the cell's candidates (the 3 cells of each neighbour row, in row order) as staged
-// indices, then lanes (target, stride q) walk that list. Every target also meets itself
-// (r^2 = 0, term h^6, count 1); that term is removed after the sum instead of testing the
-// index of every candidate. Each lane records its in-range candidates (the target itself
-// included) as staged indices in its own sub-list of nbr[gi][NBR_CAP] (in candidate order,
-// NBR_END-terminated); the lists' lengths are the counts the reference's count > 2 test uses;
-// nbr_flag[gi] = 1 when a sub-list overflowed or the brick could not be staged.
+// clCalculateDensity does (libCL/phys/oclFluid3D.cl:189-199). A warp takes a target cell and
+// up to GROUP_MAX of its particles at a time; lanes (target ti, stride q) walk the 9 (or 3)
+// neighbour rows of the cell (3 consecutive cells each, contiguous in the staging buffer),
+// lane q taking candidates q, q + Q, ... of every row, so candidate loads are shared-memory
+// broadcasts. Every target also meets itself (r^2 = 0, term h^6, count 1); that term is
+// removed after the sum instead of testing the index of every candidate. Each lane records
+// its in-range candidates (the target itself included) as staged indices in its own
+// sub-list of nbr[gi][NBR_CAP] (in candidate order, NBR_END-terminated); the lists' lengths
+// are the counts the reference's count > 2 test uses; nbr_flag[gi] = 1 when a sub-list
+// overflowed or the brick could not be staged.
 template <int DIMS, bool BATCH>
 __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
                                                                  float4* __restrict__ svel,
@@ -659,20 +688,19 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                                                                  uint8_t* __restrict__ nbr_flag, uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;  // the brick's own row
-    extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, per-warp candidate lists, per-warp neighbour lists
+    extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, then per-warp neighbour lists
     __shared__ BrickShared S;
+    __shared__ LaneMap L;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    uint16_t* clist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * CELL_LIST_MAX;
-    uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + BRICK_WARPS * CELL_LIST_MAX + warp * GROUP_MAX * WLIST_STRIDE;
+    uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * GROUP_MAX * WLIST_STRIDE;
+    lane_map_init(L);
     if (t == 0) {
         mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
         fence_mbar_init();
     }
-    __syncthreads();
     uint32_t phase = 0;
     const uint32_t n_bricks = counters[0];
     const float h2 = kp.h2, thr = kp.r2_thresh;
-    const uint32_t lt = lanemask_lt();
     // the next brick's id is fetched while this one is processed
     if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
     for (;;) {
@@ -687,35 +715,26 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
         if (staged && !brick_wait(S, phase, err)) return;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
-            uint32_t T = 0;
-            if (staged) {
-                for (int r = 0; r < R; ++r) {
-                    const uint32_t s0 = S.base[r] + S.off[r][c], len = S.off[r][c + 3] - S.off[r][c];
-                    if (T + len <= CELL_LIST_MAX)
-                        for (uint32_t k = lane; k < len; k += 32) clist[T + k] = (uint16_t)(s0 + k);
-                    T += len;
-                }
-                __syncwarp();
-            }
-            const bool flat = staged && T <= CELL_LIST_MAX;
             for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
-                const uint32_t tg = min(GROUP_MAX, nt - g0), Q = 32u / tg;
-                const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
+                const uint32_t tg = min(GROUP_MAX, nt - g0);
+                const uint32_t e = L.tq[tg][lane], f = L.info[tg];
+                const uint32_t ti = e & 0xFFu, q = e >> 8, Q = f & 0xFFu, sub = f >> 8;
                 const bool active = q < Q;
                 const uint32_t tl = t0 + g0 + ti;
                 const uint32_t gi = S.lo[RC] + tl;
                 const float4 pi = staged ? s_buf[S.base[RC] + tl] : spos[gi];
-                const uint32_t sub = nbr_sub(Q);
                 uint16_t* my = wlist + ti * WLIST_STRIDE + q * sub;
                 float acc = 0.0f;
                 uint32_t nk = 0;  // in-range candidates of this lane (the target itself included)
-                bool ovf = !flat;
                 if (active) {
-                    if (flat) {
+#pragma unroll 1
+                    for (int r = 0; r < R; ++r) {
+                        const uint32_t lo = S.off[r][c], len = S.off[r][c + 3] - lo;
+                        const float4* rp = staged ? s_buf + S.base[r] + lo : spos + S.lo[r] + lo;
+                        const uint32_t s0 = S.base[r] + lo;
 #pragma unroll 4
-                        for (uint32_t k = q; k < T; k += Q) {
-                            const uint32_t idx = clist[k];
-                            const float4 pj = s_buf[idx];
+                        for (uint32_t k = q; k < len; k += Q) {
+                            const float4 pj = rp[k];
                             const float dx = pi.x - pj.x, dy = pi.y - pj.y;
                             float r2 = fmaf(dy, dy, dx * dx);
                             if (DIMS == 3) {
@@ -730,43 +749,21 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                             // Once the sub-list is full, later candidates overwrite its last
                             // entry, so a full sub-list counts as an overflow. The target and
                             // coincident particles (r^2 = 0) are listed; the force pass skips them.
-                            my[min(nk, sub - 1)] = (uint16_t)idx;
+                            my[min(nk, sub - 1)] = (uint16_t)(s0 + k);
                             nk += in ? 1u : 0u;
                         }
-                        if (nk < sub) my[nk] = NBR_END;
-                        ovf = nk >= sub;
-                    } else {
-#pragma unroll 1
-                        for (int r = 0; r < R; ++r) {
-                            const float4* rp = staged ? s_buf + S.base[r] : spos + S.lo[r];
-                            const uint32_t hi = S.off[r][c + 3];
-                            for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
-                                const float4 pj = rp[j];
-                                const float dx = pi.x - pj.x, dy = pi.y - pj.y;
-                                float r2 = fmaf(dy, dy, dx * dx);
-                                if (DIMS == 3) {
-                                    const float dz = pi.z - pj.z;
-                                    r2 = fmaf(dz, dz, r2);
-                                }
-                                const bool in = r2 < thr;
-                                const float tt = in ? h2 - r2 : 0.0f;
-                                acc = fmaf(tt * tt, tt, acc);
-                                nk += in ? 1u : 0u;
-                            }
-                        }
                     }
+                    if (nk < sub) my[nk] = NBR_END;
                 }
+                const bool ovf = !staged || nk >= sub;
                 acc = reduce_q(acc, q, Q, tg);
-                float cnt = reduce_q((float)nk, q, Q, tg);
-                uint32_t gm = 0;  // lanes sharing this lane's target
-                for (uint32_t k = 0; k < Q; ++k) gm |= 1u << (ti + k * tg);
-                const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & gm;
-                (void)lt;
+                const float cnt = reduce_q((float)nk, q, Q, tg);
+                const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & (L.group[tg] << ti);
                 if (active && q == 0) {
                     acc -= h2 * h2 * h2;  // the target's own term
-                    cnt -= 1.0f;
+                    const float count = cnt - 1.0f;
                     float rho = kp.rho0, p = kp.p0;
-                    if (cnt > 2.5f) {
+                    if (count > 2.5f) {
                         rho = fmaxf(1.0f, kp.mass * kp.kconst * acc);
                         p = kp.p0 + S.stiff * (rho - kp.rho0);
                     }
@@ -774,17 +771,23 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                     reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
                     nbr_flag[gi] = om ? 1 : 0;
                 }
-                // copy the group's lists (tg consecutive particles) out with 16-byte stores
+                // copy the group's lists out. A brick's lists fill the brick's targets' rows of
+                // nbr, stored chunk-major: the 16-byte chunk ch (entries 8ch..8ch+7) of the
+                // brick's u-th target is uint4 number ch * ntarg + u (so that the force pass,
+                // one lane per target, reads consecutive chunks); half-warps copy one chunk of
+                // up to 16 consecutive targets each.
                 __syncwarp();
-                if (flat) {
-                    const uint32_t* src = reinterpret_cast<const uint32_t*>(wlist);
-                    uint32_t* dst = reinterpret_cast<uint32_t*>(nbr + (size_t)(S.lo[RC] + t0 + g0) * NBR_CAP);
-                    for (uint32_t tt = 0; tt < tg; ++tt)  // NBR_CAP / 2 = 32 words per target
-                        dst[tt * (NBR_CAP / 2) + lane] = src[tt * (WLIST_STRIDE / 2) + lane];
+                if (staged) {
+                    const uint32_t u0 = t0 + g0 - S.off[RC][1], ntarg = S.off[RC][ncell + 1] - S.off[RC][1];
+                    uint4* dst = reinterpret_cast<uint4*>(nbr + (size_t)(S.lo[RC] + S.off[RC][1]) * NBR_CAP);
+                    const uint32_t row = (uint32_t)lane & 15u;
+                    if (row < tg)
+                        for (uint32_t ch = (uint32_t)lane >> 4; ch < NBR_CAP / 8; ch += 2)
+                            dst[(size_t)ch * ntarg + u0 + row] =
+                                *reinterpret_cast<const uint4*>(wlist + row * WLIST_STRIDE + ch * 8u);
                 }
                 __syncwarp();
             }
-            __syncwarp();  // clist is rebuilt for the warp's next cell
         }
         if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
@@ -811,6 +814,13 @@ __device__ __forceinline__ void force_pair(const float4& pi, const float4& vi, f
     acc[5] = fmaf(vj.z - vi.z, cv, acc[5]);
 }
 
+// Reciprocal with the approximate (about 1 ulp) hardware instruction.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // force_pair on the force pass's staged copies, whose w lanes hold a = 1/rho (positions) and
 // b = p/rho (velocities): (p_i + p_j) / (rho_i rho_j) = b_i a_j + a_i b_j. Skips r = 0 (the
 // target itself, which its list holds, and coincident particles).
@@ -835,13 +845,13 @@ __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& v
 }
 
 // Forces (pressure + viscosity) for every particle of the occupied bricks. The brick's rows
-// are staged exactly as in k_density_brick, and each lane evaluates only the in-range pairs
-// that the density kernel recorded in its sub-list. Targets whose lists are unusable
+// are staged exactly as in k_density_brick; each lane takes one target and evaluates the
+// in-range pairs that the density kernel recorded in the target's sub-lists. Targets whose lists are unusable
 // (overflow, unstaged brick) are handled by scanning the rows. With FUSED the clip-box,
 // integrate-force, gravity and integrate-velocity stages follow in registers; otherwise the
 // SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
 template <int DIMS, bool FUSED, bool BATCH>
-__global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __restrict__ spos,
+__global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* __restrict__ spos,
                                                                const float4* __restrict__ svel,
                                                                const uint32_t* __restrict__ index,
                                                                float4* __restrict__ pos,
@@ -859,12 +869,13 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
     // LIST_STAGE_MAX targets
     extern __shared__ float4 s_buf[];
     __shared__ BrickShared S;
+    __shared__ LaneMap L;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    lane_map_init(L);
     if (t == 0) {
         mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
         fence_mbar_init();
     }
-    __syncthreads();
     uint32_t phase = 0;
     const uint32_t n_bricks = counters[0];
     const float4* s_pos = s_buf;
@@ -909,54 +920,59 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
             if (!brick_wait(S, phase, err)) return;
             // w lanes of the staged copies: 1/rho and p/rho (force_pair_pre)
             for (uint32_t k = t; k < S.total; k += BRICK_THREADS) {
-                const float a = __frcp_rn(s_buf[k].w);
+                const float a = rcp_approx(s_buf[k].w);
                 s_buf[k].w = a;
                 s_buf[BRICK_CAP + k].w *= a;
             }
             __syncthreads();
         }
-        for (int c = warp; c < ncell; c += BRICK_WARPS) {
-            const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
-            // the same target groups as the density pass: its lists are split into sub-lists
-            // by the group's lane count
-            for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
-                const uint32_t tg = min(GROUP_MAX, nt - g0), Q = 32u / tg;
-                const uint32_t ti = (uint32_t)lane % tg, q = (uint32_t)lane / tg;
-                const bool active = q < Q;
-                const uint32_t tl = t0 + g0 + ti;
-                const uint32_t gi = S.lo[RC] + tl;
-                const float4 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
-                const float4 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
-                const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
-                float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-                // prefetch what the integration needs so its latency overlaps the pair loop
-                uint32_t o = 0;
-                float4 f_o = make_float4(0.f, 0.f, 0.f, 0.f), v_o = f_o, p_o = f_o;
-                if (active && q == 0) {
-                    o = index[gi];
-                    f_o = force[o];
-                    if (FUSED) {
-                        v_o = vel[o];
-                        p_o = pos[o];
-                    }
-                }
-                const bool scan = !staged || nbr_flag[gi] != 0;
-                if (active && !scan) {
-                    const uint32_t sub = nbr_sub(Q);
-                    const uint16_t* my = (lists_staged ? s_lists + (size_t)(gi - tfirst) * NBR_CAP
-                                                       : nbr + (size_t)gi * NBR_CAP) + q * sub;
+        // one lane per target: the brick's targets are consecutive in the centre row, so a warp
+        // takes 32 of them at a time whatever cell they are in
+        const uint32_t tbeg = S.off[RC][1], tend = S.off[RC][ncell + 1];
+        for (uint32_t tb = tbeg + (uint32_t)warp * 32u; tb < tend; tb += BRICK_WARPS * 32u) {
+            const uint32_t tl = tb + (uint32_t)lane;
+            if (tl >= tend) break;
+            // the target's cell and its place in the density pass's groups (its sub-lists)
+            int c = 0;
+            while (c + 1 < ncell && S.off[RC][c + 2] <= tl) ++c;
+            const uint32_t c0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - c0;
+            const uint32_t g0 = (tl - c0) & ~(GROUP_MAX - 1u);
+            const uint32_t f = L.info[min(GROUP_MAX, nt - g0)];
+            const uint32_t Q = f & 0xFFu, sub = f >> 8;
+            const uint32_t gi = S.lo[RC] + tl;
+            const float4 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
+            const float4 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
+            const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
+            float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            // prefetch what the integration needs so its latency overlaps the pair loop
+            const uint32_t o = index[gi];
+            const float4 f_o = force[o];
+            float4 v_o = f_o, p_o = f_o;
+            if (FUSED) {
+                v_o = vel[o];
+                p_o = pos[o];
+            }
+            const bool scan = !staged || nbr_flag[gi] != 0;
+            if (!scan) {
+                // chunk ch of this target's list (the density pass's chunk-major layout)
+                const uint4* lst = (lists_staged ? reinterpret_cast<const uint4*>(s_lists)
+                                                 : reinterpret_cast<const uint4*>(nbr + (size_t)tfirst * NBR_CAP)) +
+                                   (gi - tfirst);
+#pragma unroll 1
+                for (uint32_t q = 0; q < Q; ++q) {
                     bool done = false;
                     for (uint32_t k0 = 0; k0 < sub && !done; k0 += 8) {
-                        uint32_t w[4];  // up to 8 entries, two per word
-                        if (sub >= 8) {
-                            const uint4 v = *reinterpret_cast<const uint4*>(my + k0);
-                            w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
-                        } else if (sub == 4) {
-                            const uint2 v = *reinterpret_cast<const uint2*>(my);
-                            w[0] = v.x; w[1] = v.y; w[2] = w[3] = 0xFFFFFFFFu;
-                        } else {
-                            w[0] = *reinterpret_cast<const uint32_t*>(my);
-                            w[1] = w[2] = w[3] = 0xFFFFFFFFu;
+                        const uint32_t e0 = q * sub + k0;  // first entry of this piece
+                        const uint4 v = lst[(size_t)(e0 >> 3) * ntarg];
+                        uint32_t w[4] = {v.x, v.y, v.z, v.w};  // up to 8 entries, two per word
+                        if (sub < 8) {  // 4 or 2 entries of the chunk are this sub-list's
+                            if (e0 & 4u) {
+                                w[0] = w[2];
+                                w[1] = w[3];
+                            }
+                            if (e0 & 2u) w[0] = w[1];
+                            w[2] = w[3] = 0xFFFFFFFFu;
+                            if (sub == 2) w[1] = 0xFFFFFFFFu;
                         }
 #pragma unroll
                         for (int e = 0; e < 8; ++e) {
@@ -968,47 +984,43 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_force_brick(const float4* __r
                             force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
                         }
                     }
-                } else if (active) {
+                }
+            } else {
 #pragma unroll 1
-                    for (int r = 0; r < R; ++r) {
-                        const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
-                        const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
-                        const uint32_t hi = S.off[r][c + 3];
-                        for (uint32_t j = S.off[r][c] + q; j < hi; j += Q) {
-                            const float4 pj = rp[j];
-                            const float dx = pi.x - pj.x, dy = pi.y - pj.y;
-                            float r2 = fmaf(dy, dy, dx * dx);
-                            if (DIMS == 3) {
-                                const float dz = pi.z - pj.z;
-                                r2 = fmaf(dz, dz, r2);
-                            }
-                            if (r2 < kp.r2_thresh && r2 > 0.0f) {
-                                if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
-                                else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
-                            }
+                for (int r = 0; r < R; ++r) {
+                    const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
+                    const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
+                    const uint32_t hi = S.off[r][c + 3];
+                    for (uint32_t j = S.off[r][c]; j < hi; ++j) {
+                        const float4 pj = rp[j];
+                        const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                        float r2 = fmaf(dy, dy, dx * dx);
+                        if (DIMS == 3) {
+                            const float dz = pi.z - pj.z;
+                            r2 = fmaf(dz, dz, r2);
+                        }
+                        if (r2 < kp.r2_thresh && r2 > 0.0f) {
+                            if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
+                            else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
                         }
                     }
                 }
-#pragma unroll
-                for (int k = 0; k < 6; ++k) acc[k] = reduce_q(acc[k], q, Q, tg);
-                if (active && q == 0) {
-                    float4 f = f_o;
-                    const float cvisc = S.cvisc;
-                    f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(cvisc, acc[3])), kp.mass));
-                    f.y = __fadd_rn(f.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(cvisc, acc[4])), kp.mass));
-                    f.z = __fadd_rn(f.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(cvisc, acc[5])), kp.mass));
-                    f.w = 0.0f;
-                    if (FUSED) {
-                        f = clip_box_force(kp, S.box_min, S.box_max, pi, vi, f);
-                        if (kp.rec_force) kp.rec_force[o] = f;
-                        const float4 v = integrate_force(kp, v_o, f);
-                        vel[o] = v;
-                        force[o] = kp.gravity;
-                        pos[o] = integrate_velocity(kp, p_o, v);
-                    } else {
-                        force[o] = f;
-                    }
-                }
+            }
+            float4 fs = f_o;
+            const float cvisc = S.cvisc;
+            fs.x = __fadd_rn(fs.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(cvisc, acc[3])), kp.mass));
+            fs.y = __fadd_rn(fs.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(cvisc, acc[4])), kp.mass));
+            fs.z = __fadd_rn(fs.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(cvisc, acc[5])), kp.mass));
+            fs.w = 0.0f;
+            if (FUSED) {
+                fs = clip_box_force(kp, S.box_min, S.box_max, pi, vi, fs);
+                if (kp.rec_force) kp.rec_force[o] = fs;
+                const float4 v = integrate_force(kp, v_o, fs);
+                vel[o] = v;
+                force[o] = kp.gravity;
+                pos[o] = integrate_velocity(kp, p_o, v);
+            } else {
+                force[o] = fs;
             }
         }
         if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
