@@ -926,101 +926,116 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
             }
             __syncthreads();
         }
-        // one lane per target: the brick's targets are consecutive in the centre row, so a warp
-        // takes 32 of them at a time whatever cell they are in
-        const uint32_t tbeg = S.off[RC][1], tend = S.off[RC][ncell + 1];
-        for (uint32_t tb = tbeg + (uint32_t)warp * 32u; tb < tend; tb += BRICK_WARPS * 32u) {
-            const uint32_t tl = tb + (uint32_t)lane;
-            if (tl >= tend) break;
-            // the target's cell and its place in the density pass's groups (its sub-lists)
-            int c = 0;
-            while (c + 1 < ncell && S.off[RC][c + 2] <= tl) ++c;
-            const uint32_t c0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - c0;
-            const uint32_t g0 = (tl - c0) & ~(GROUP_MAX - 1u);
-            const uint32_t f = L.info[min(GROUP_MAX, nt - g0)];
-            const uint32_t Q = f & 0xFFu, sub = f >> 8;
+        // P = 4 lanes per target: the brick's targets are consecutive in the centre row, so the
+        // CTA takes 64 of them at a time whatever cell they are in; lane p of a target takes
+        // its sub-lists p, p + 4, ... (or, scanning, every 4th candidate of each row) and the 4
+        // partial sums are added with shuffles. The summation order depends on neither the
+        // brick width nor the brick's target count.
+        const uint32_t tbeg = S.off[RC][1];
+        constexpr uint32_t lp = 2u, P = 1u << lp;
+        for (uint32_t u0 = 0; u0 < ntarg; u0 += BRICK_THREADS >> lp) {
+            const uint32_t u = u0 + ((uint32_t)t >> lp), p = (uint32_t)t & (P - 1u);
+            const bool active = u < ntarg;
+            const uint32_t tl = tbeg + u;
             const uint32_t gi = S.lo[RC] + tl;
-            const float4 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
-            const float4 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
-            const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
             float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-            // prefetch what the integration needs so its latency overlaps the pair loop
-            const uint32_t o = index[gi];
-            const float4 f_o = force[o];
-            float4 v_o = f_o, p_o = f_o;
-            if (FUSED) {
-                v_o = vel[o];
-                p_o = pos[o];
-            }
-            const bool scan = !staged || nbr_flag[gi] != 0;
-            if (!scan) {
-                // chunk ch of this target's list (the density pass's chunk-major layout)
-                const uint4* lst = (lists_staged ? reinterpret_cast<const uint4*>(s_lists)
-                                                 : reinterpret_cast<const uint4*>(nbr + (size_t)tfirst * NBR_CAP)) +
-                                   (gi - tfirst);
+            float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = pi, f_o = pi, v_o = pi, p_o = pi;
+            uint32_t o = 0;
+            if (active) {
+                // the target's cell and its place in the density pass's groups (its sub-lists)
+                int c = 0;
+                while (c + 1 < ncell && S.off[RC][c + 2] <= tl) ++c;
+                const uint32_t c0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - c0;
+                const uint32_t g0 = (tl - c0) & ~(GROUP_MAX - 1u);
+                const uint32_t f = L.info[min(GROUP_MAX, nt - g0)];
+                const uint32_t Q = f & 0xFFu, sub = f >> 8;
+                pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
+                vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
+                const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
+                if (p == 0) {  // prefetch what the integration needs
+                    o = index[gi];
+                    f_o = force[o];
+                    if (FUSED) {
+                        v_o = vel[o];
+                        p_o = pos[o];
+                    }
+                }
+                const bool scan = !staged || nbr_flag[gi] != 0;
+                if (!scan) {
+                    // chunk ch of this target's list (the density pass's chunk-major layout)
+                    const uint4* lst = (lists_staged ? reinterpret_cast<const uint4*>(s_lists)
+                                                     : reinterpret_cast<const uint4*>(nbr + (size_t)tfirst * NBR_CAP)) +
+                                       (gi - tfirst);
 #pragma unroll 1
-                for (uint32_t q = 0; q < Q; ++q) {
-                    bool done = false;
-                    for (uint32_t k0 = 0; k0 < sub && !done; k0 += 8) {
-                        const uint32_t e0 = q * sub + k0;  // first entry of this piece
-                        const uint4 v = lst[(size_t)(e0 >> 3) * ntarg];
-                        uint32_t w[4] = {v.x, v.y, v.z, v.w};  // up to 8 entries, two per word
-                        if (sub < 8) {  // 4 or 2 entries of the chunk are this sub-list's
-                            if (e0 & 4u) {
-                                w[0] = w[2];
-                                w[1] = w[3];
+                    for (uint32_t q = p; q < Q; q += P) {
+                        bool done = false;
+                        for (uint32_t k0 = 0; k0 < sub && !done; k0 += 8) {
+                            const uint32_t e0 = q * sub + k0;  // first entry of this piece
+                            const uint4 v = lst[(size_t)(e0 >> 3) * ntarg];
+                            uint32_t w[4] = {v.x, v.y, v.z, v.w};  // up to 8 entries, two per word
+                            if (sub < 8) {  // 4 or 2 entries of the chunk are this sub-list's
+                                if (e0 & 4u) {
+                                    w[0] = w[2];
+                                    w[1] = w[3];
+                                }
+                                if (e0 & 2u) w[0] = w[1];
+                                w[2] = w[3] = 0xFFFFFFFFu;
+                                if (sub == 2) w[1] = 0xFFFFFFFFu;
                             }
-                            if (e0 & 2u) w[0] = w[1];
-                            w[2] = w[3] = 0xFFFFFFFFu;
-                            if (sub == 2) w[1] = 0xFFFFFFFFu;
-                        }
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) {
-                            const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-                            if (idx == NBR_END) {
-                                done = true;
-                                break;
+                            for (int e = 0; e < 8; ++e) {
+                                const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                                if (idx == NBR_END) {
+                                    done = true;
+                                    break;
+                                }
+                                force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
                             }
-                            force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
                         }
                     }
-                }
-            } else {
+                } else {
 #pragma unroll 1
-                for (int r = 0; r < R; ++r) {
-                    const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
-                    const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
-                    const uint32_t hi = S.off[r][c + 3];
-                    for (uint32_t j = S.off[r][c]; j < hi; ++j) {
-                        const float4 pj = rp[j];
-                        const float dx = pi.x - pj.x, dy = pi.y - pj.y;
-                        float r2 = fmaf(dy, dy, dx * dx);
-                        if (DIMS == 3) {
-                            const float dz = pi.z - pj.z;
-                            r2 = fmaf(dz, dz, r2);
-                        }
-                        if (r2 < kp.r2_thresh && r2 > 0.0f) {
-                            if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
-                            else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
+                    for (int r = 0; r < R; ++r) {
+                        const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
+                        const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
+                        const uint32_t hi = S.off[r][c + 3];
+                        for (uint32_t j = S.off[r][c] + p; j < hi; j += P) {
+                            const float4 pj = rp[j];
+                            const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                            float r2 = fmaf(dy, dy, dx * dx);
+                            if (DIMS == 3) {
+                                const float dz = pi.z - pj.z;
+                                r2 = fmaf(dz, dz, r2);
+                            }
+                            if (r2 < kp.r2_thresh && r2 > 0.0f) {
+                                if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
+                                else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
+                            }
                         }
                     }
                 }
             }
-            float4 fs = f_o;
-            const float cvisc = S.cvisc;
-            fs.x = __fadd_rn(fs.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(cvisc, acc[3])), kp.mass));
-            fs.y = __fadd_rn(fs.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(cvisc, acc[4])), kp.mass));
-            fs.z = __fadd_rn(fs.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(cvisc, acc[5])), kp.mass));
-            fs.w = 0.0f;
-            if (FUSED) {
-                fs = clip_box_force(kp, S.box_min, S.box_max, pi, vi, fs);
-                if (kp.rec_force) kp.rec_force[o] = fs;
-                const float4 v = integrate_force(kp, v_o, fs);
-                vel[o] = v;
-                force[o] = kp.gravity;
-                pos[o] = integrate_velocity(kp, p_o, v);
-            } else {
-                force[o] = fs;
+            for (uint32_t m = P >> 1; m > 0; m >>= 1) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], m);
+            }
+            if (active && p == 0) {
+                float4 fs = f_o;
+                const float cvisc = S.cvisc;
+                fs.x = __fadd_rn(fs.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[0]), __fmul_rn(cvisc, acc[3])), kp.mass));
+                fs.y = __fadd_rn(fs.y, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[1]), __fmul_rn(cvisc, acc[4])), kp.mass));
+                fs.z = __fadd_rn(fs.z, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, acc[2]), __fmul_rn(cvisc, acc[5])), kp.mass));
+                fs.w = 0.0f;
+                if (FUSED) {
+                    fs = clip_box_force(kp, S.box_min, S.box_max, pi, vi, fs);
+                    if (kp.rec_force) kp.rec_force[o] = fs;
+                    const float4 v = integrate_force(kp, v_o, fs);
+                    vel[o] = v;
+                    force[o] = kp.gravity;
+                    pos[o] = integrate_velocity(kp, p_o, v);
+                } else {
+                    force[o] = fs;
+                }
             }
         }
         if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
