@@ -29,7 +29,7 @@ struct gbsph_batch3d_s {
     uint32_t *keys_a = nullptr, *keys_b = nullptr, *keys_c = nullptr, *vals_a = nullptr, *vals_b = nullptr;
     uint32_t *index = nullptr, *bricks = nullptr;
     uint16_t* nbr = nullptr;
-    uint8_t* nbr_flag = nullptr;
+    uint64_t* nbr_meta = nullptr;
     uint2* table = nullptr;
     bool table_clean = false;
     void* scratch = nullptr;
@@ -162,9 +162,9 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     h->table_clean = true;
     k_density_brick<3, true><<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks,
-                                                                                bcounters(h), kp, h->nbr, h->nbr_flag, h->err);
+                                                                                bcounters(h), kp, h->nbr, h->nbr_meta, h->err);
     k_force_brick<3, true, true><<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(
-        h->spos, h->svel, h->index, h->pos, h->vel, h->force, h->table, h->bricks, bcounters(h), kp, h->nbr, h->nbr_flag,
+        h->spos, h->svel, h->index, h->pos, h->vel, h->force, h->table, h->bricks, bcounters(h), kp, h->nbr, h->nbr_meta,
         h->err);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
@@ -303,7 +303,7 @@ GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_pa
     h->n = n;
     h->cells = cells;
     const size_t n4 = (n + 63) & ~size_t(63);
-    const size_t bytes = n4 * (5 * 16 + 7 * 4 + NBR_CAP * 2 + 1);
+    const size_t bytes = n4 * (5 * 16 + 7 * 4 + NBR_CAP * 2 + 8);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->block, bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->block, 0, bytes));
     char* p = (char*)h->block;
@@ -319,7 +319,7 @@ GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_pa
     }
     h->nbr = (uint16_t*)p;
     p += n4 * NBR_CAP * 2;
-    h->nbr_flag = (uint8_t*)p;
+    h->nbr_meta = (uint64_t*)p;
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->table, cells * sizeof(uint2)));
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES)));
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->sdev, n_scenes * sizeof(SceneDev)));

@@ -64,7 +64,7 @@ struct gbsph_fluid3d_s {
     uint32_t *keys_a = nullptr, *keys_b = nullptr, *keys_c = nullptr;
     uint32_t *vals_a = nullptr, *vals_b = nullptr, *index = nullptr, *bricks = nullptr;
     uint16_t* nbr = nullptr;      // per particle NBR_CAP neighbour slots (density -> forces)
-    uint8_t* nbr_flag = nullptr;  // per particle: 1 = scan instead of the list
+    uint64_t* nbr_meta = nullptr;  // per particle: sub-list lengths, scan flag (bit 63)
     uint32_t* hash_tables = nullptr;  // cell start / end, REF_BUCKETS each
     uint2* table = nullptr;           // LINEAR_GRID interleaved table
     size_t table_cells = 0;
@@ -200,7 +200,7 @@ void free_particle_arrays(H* h) {
 int alloc_particle_arrays(H* h, size_t n) {
     free_particle_arrays(h);
     const size_t n4 = (n + 63) & ~size_t(63);
-    const size_t bytes = n4 * (2 * 16 + 7 * 4 + NBR_CAP * 2 + 1);
+    const size_t bytes = n4 * (2 * 16 + 7 * 4 + NBR_CAP * 2 + 8);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->pblock, bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->pblock, 0, bytes));
     char* p = (char*)h->pblock;
@@ -215,7 +215,7 @@ int alloc_particle_arrays(H* h, size_t n) {
     }
     h->nbr = (uint16_t*)p;
     p += n4 * NBR_CAP * 2;
-    h->nbr_flag = (uint8_t*)p;
+    h->nbr_meta = (uint64_t*)p;
     h->scratch_bytes = onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, h->scratch_bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->scratch, 0, h->scratch_bytes));
@@ -343,7 +343,7 @@ int st_forces_exact(H* h, const KParams& kp, cudaStream_t s) {
 int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
     auto launch = [&](auto kern) {
         kern<<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp,
-                                                                 h->nbr, h->nbr_flag, h->err);
+                                                                 h->nbr, h->nbr_meta, h->err);
     };
     if (kp.dims == 2) launch(k_density_brick<2, false>);
     else launch(k_density_brick<3, false>);
@@ -355,7 +355,7 @@ int st_force_brick(H* h, const KParams& kp, cudaStream_t s, bool fused) {
     auto launch = [&](auto kern) {
         kern<<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2),
                                                                 h->table, h->bricks, counters(h), kp, h->nbr,
-                                                                h->nbr_flag, h->err);
+                                                                h->nbr_meta, h->err);
     };
     if (kp.dims == 2) {
         if (fused) launch(k_force_brick<2, true, false>);

@@ -620,25 +620,24 @@ __device__ __forceinline__ float reduce_q(float v, uint32_t q, uint32_t Q, uint3
 // records are indices into that staging.
 constexpr uint32_t BRICK_CAP = 1536;
 constexpr uint32_t NBR_CAP = 64;         // neighbour slots per particle (uint16), split over the Q lanes
-constexpr uint16_t NBR_END = 0xFFFFu;    // terminates a lane's neighbour sub-list
 constexpr uint32_t WLIST_STRIDE = NBR_CAP + 8;  // shared-memory stride per target (halves; 16-byte rows)
 constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists the force kernel stages
 constexpr uint32_t GROUP_MAX = 16;              // targets a warp takes at once (both passes)
+constexpr uint32_t NBR_SUBLISTS = 8;            // at most 8 lanes (sub-lists) per target
+constexpr uint64_t NBR_SCAN = 1ull << 63;       // nbr_meta: the force pass scans for this target
 
 
 // Dynamic shared memory of the brick kernels.
 constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * GROUP_MAX * WLIST_STRIDE * 2;
 constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
 
-// Slots of each lane's sub-list when Q lanes share a target: a multiple of 8 (one 16-byte
-// vector) when Q <= 8, else 4 or 2, so sub-lists start on their load width.
-__device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) {
-    const uint32_t s = NBR_CAP / Q;
-    return s >= 8 ? (s & ~7u) : (s >= 4 ? 4u : 2u);
-}
+// Slots of each lane's sub-list when Q lanes share a target: sub-list q holds slots
+// [q * sub, (q + 1) * sub) of the target's NBR_CAP slots.
+__device__ __forceinline__ uint32_t nbr_sub(uint32_t Q) { return NBR_CAP / Q; }
 
 // Lane layout of a group of tg targets (1 <= tg <= GROUP_MAX) on a warp: lane = q * tg + ti
-// serves target ti with stride q of Q = 32 / tg (lanes with q >= Q idle). tq packs ti | q << 8;
+// serves target ti with stride q of Q = min(32 / tg, NBR_SUBLISTS) (lanes with q >= Q idle).
+// tq packs ti | q << 8;
 // info packs Q | nbr_sub(Q) << 8; group << ti is the mask of the lanes serving target ti.
 // Both neighbour passes use it, so the density pass's sub-lists are the force pass's.
 struct LaneMap {
@@ -655,7 +654,7 @@ __device__ __forceinline__ void lane_map_init(LaneMap& L) {
             if (lane == 0) L.info[0] = L.group[0] = 0;
             continue;
         }
-        const uint32_t Q = 32 / tg;
+        const uint32_t Q = min(32 / tg, NBR_SUBLISTS);
         L.tq[tg][lane] = (uint16_t)((lane % tg) | ((lane / tg) << 8));
         if (lane == 0) {
             uint32_t m = 0;
@@ -675,22 +674,23 @@ __device__ __forceinline__ void lane_map_init(LaneMap& L) {
 // broadcasts. Every target also meets itself (r^2 = 0, term h^6, count 1); that term is
 // removed after the sum instead of testing the index of every candidate. Each lane records
 // its in-range candidates (the target itself included) as staged indices in its own
-// sub-list of nbr[gi][NBR_CAP] (in candidate order, NBR_END-terminated); the lists' lengths
-// are the counts the reference's count > 2 test uses; nbr_flag[gi] = 1 when a sub-list
-// overflowed or the brick could not be staged.
+// sub-list of nbr[gi][NBR_CAP] (in candidate order); the lists' lengths are the counts the
+// reference's count > 2 test uses and go to nbr_meta[gi] (one byte per sub-list), or
+// nbr_meta[gi] = NBR_SCAN when a sub-list overflowed or the brick could not be staged.
 template <int DIMS, bool BATCH>
-__global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restrict__ spos,
+__global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __restrict__ spos,
                                                                  float4* __restrict__ svel,
                                                                  const uint2* __restrict__ table,
                                                                  const uint32_t* __restrict__ bricks,
                                                                  uint32_t* counters, KParams kp,
                                                                  uint16_t* __restrict__ nbr,
-                                                                 uint8_t* __restrict__ nbr_flag, uint32_t* err) {
+                                                                 uint64_t* __restrict__ nbr_meta, uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;  // the brick's own row
     extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, then per-warp neighbour lists
     __shared__ BrickShared S;
     __shared__ LaneMap L;
+    __shared__ __align__(8) uint8_t wcnt[BRICK_WARPS][GROUP_MAX][NBR_SUBLISTS];  // sub-list lengths
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * GROUP_MAX * WLIST_STRIDE;
     lane_map_init(L);
@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                             const float tt = in ? h2 - r2 : 0.0f;
                             acc = fmaf(tt * tt, tt, acc);
                             // branch-free append: the slot after the last real entry is
-                            // overwritten by the next candidate or by the terminator below.
+                            // overwritten by the next candidate.
                             // Once the sub-list is full, later candidates overwrite its last
                             // entry, so a full sub-list counts as an overflow. The target and
                             // coincident particles (r^2 = 0) are listed; the force pass skips them.
@@ -753,12 +753,14 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                             nk += in ? 1u : 0u;
                         }
                     }
-                    if (nk < sub) my[nk] = NBR_END;
                 }
                 const bool ovf = !staged || nk >= sub;
                 acc = reduce_q(acc, q, Q, tg);
                 const float cnt = reduce_q((float)nk, q, Q, tg);
                 const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & (L.group[tg] << ti);
+                // the target's sub-list lengths, one byte each, gathered through shared memory
+                if (active) wcnt[warp][ti][q] = (uint8_t)min(nk, 127u);
+                __syncwarp();
                 if (active && q == 0) {
                     acc -= h2 * h2 * h2;  // the target's own term
                     const float count = cnt - 1.0f;
@@ -769,7 +771,8 @@ __global__ void __launch_bounds__(BRICK_THREADS) k_density_brick(float4* __restr
                     }
                     spos[gi] = make_float4(pi.x, pi.y, pi.z, rho);
                     reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
-                    nbr_flag[gi] = om ? 1 : 0;
+                    const uint64_t lens = *reinterpret_cast<const uint64_t*>(wcnt[warp][ti]);
+                    nbr_meta[gi] = om ? NBR_SCAN : (Q < 8 ? lens & ((1ull << (8 * Q)) - 1ull) : lens);
                 }
                 // copy the group's lists out. A brick's lists fill the brick's targets' rows of
                 // nbr, stored chunk-major: the 16-byte chunk ch (entries 8ch..8ch+7) of the
@@ -861,7 +864,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                                                                const uint32_t* __restrict__ bricks,
                                                                uint32_t* counters, KParams kp,
                                                                const uint16_t* __restrict__ nbr,
-                                                               const uint8_t* __restrict__ nbr_flag,
+                                                               const uint64_t* __restrict__ nbr_meta,
                                                                uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;
@@ -928,7 +931,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
         }
         // P = 4 lanes per target: the brick's targets are consecutive in the centre row, so the
         // CTA takes 64 of them at a time whatever cell they are in; lane p of a target takes
-        // its sub-lists p, p + 4, ... (or, scanning, every 4th candidate of each row) and the 4
+        // every 4th entry of its list (or, scanning, every 4th candidate of each row) and the 4
         // partial sums are added with shuffles. The summation order depends on neither the
         // brick width nor the brick's target count.
         const uint32_t tbeg = S.off[RC][1];
@@ -960,38 +963,48 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                         p_o = pos[o];
                     }
                 }
-                const bool scan = !staged || nbr_flag[gi] != 0;
+                const uint64_t meta = staged ? nbr_meta[gi] : NBR_SCAN;
+                const bool scan = (meta & NBR_SCAN) != 0;
                 if (!scan) {
-                    // chunk ch of this target's list (the density pass's chunk-major layout)
-                    const uint4* lst = (lists_staged ? reinterpret_cast<const uint4*>(s_lists)
-                                                     : reinterpret_cast<const uint4*>(nbr + (size_t)tfirst * NBR_CAP)) +
-                                       (gi - tfirst);
-#pragma unroll 1
-                    for (uint32_t q = p; q < Q; q += P) {
-                        bool done = false;
-                        for (uint32_t k0 = 0; k0 < sub && !done; k0 += 8) {
-                            const uint32_t e0 = q * sub + k0;  // first entry of this piece
-                            const uint4 v = lst[(size_t)(e0 >> 3) * ntarg];
-                            uint32_t w[4] = {v.x, v.y, v.z, v.w};  // up to 8 entries, two per word
-                            if (sub < 8) {  // 4 or 2 entries of the chunk are this sub-list's
-                                if (e0 & 4u) {
-                                    w[0] = w[2];
-                                    w[1] = w[3];
-                                }
-                                if (e0 & 2u) w[0] = w[1];
-                                w[2] = w[3] = 0xFFFFFFFFu;
-                                if (sub == 2) w[1] = 0xFFFFFFFFu;
-                            }
+                    // With four sub-lists lane p takes sub-list p; otherwise the Q sub-lists
+                    // are one sequence and lane p takes its entries p, p + 4, ..., two at a time
+                    // so that their loads overlap (slot s of the target's list sits at
+                    // chunk-major position ((s >> 3) * ntarg + u) * 8 + (s & 7))
+                    const uint16_t* lst = (lists_staged ? s_lists : nbr + (size_t)tfirst * NBR_CAP) + (gi - tfirst) * 8u;
+                    const uint32_t n8 = ntarg * 8u;
+                    uint32_t before = 0;  // entries of the earlier sub-lists
+                    if (Q == P) {  // one sub-list per lane (16 slots, two 16-byte chunks)
+                        const uint32_t n = (uint32_t)(meta >> (8 * p)) & 127u;
+                        const uint4* l4 = reinterpret_cast<const uint4*>(lst);
+                        for (uint32_t k0 = 0; k0 < n; k0 += 8) {
+                            const uint4 v = l4[(size_t)((p * sub + k0) >> 3) * ntarg];
+                            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+                            const uint32_t m = min(8u, n - k0);
 #pragma unroll
-                            for (int e = 0; e < 8; ++e) {
+                            for (uint32_t e = 0; e < 8; ++e) {
+                                if (e >= m) break;
                                 const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-                                if (idx == NBR_END) {
-                                    done = true;
-                                    break;
-                                }
                                 force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
                             }
                         }
+                    }
+#pragma unroll 1
+                    for (uint32_t q = 0; q < (Q == P ? 0u : Q); ++q) {
+                        const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u, b = q * sub;
+                        uint32_t k = (p - before) & (P - 1u);
+                        for (; k + P < n; k += 2 * P) {
+                            const uint32_t s0 = b + k, s1 = s0 + P;
+                            const uint32_t i0 = lst[(s0 >> 3) * n8 + (s0 & 7u)];
+                            const uint32_t i1 = lst[(s1 >> 3) * n8 + (s1 & 7u)];
+                            force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
+                            force_pair_pre<DIMS>(pi, vi, s_pos[i1], s_vel[i1], kp.h, acc);
+                        }
+                        if (k < n) {
+                            const uint32_t s0 = b + k;
+                            const uint32_t i0 = lst[(s0 >> 3) * n8 + (s0 & 7u)];
+                            force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
+                        }
+                        before += n;
                     }
                 } else {
 #pragma unroll 1
