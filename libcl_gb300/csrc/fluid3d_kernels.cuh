@@ -629,7 +629,12 @@ constexpr uint64_t NBR_SCAN = 1ull << 63;       // nbr_meta: the force pass scan
 
 // Dynamic shared memory of the brick kernels.
 constexpr size_t DENSITY_SMEM = (size_t)BRICK_CAP * 16 + (size_t)BRICK_WARPS * GROUP_MAX * WLIST_STRIDE * 2;
-constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
+// force: staged positions and velocities, then the lists, list lengths and permutation
+// entries of up to LIST_STAGE_MAX targets (the last two rounded out to 16-byte copies)
+constexpr size_t FORCE_LIST_BYTES = (size_t)LIST_STAGE_MAX * NBR_CAP * 2;
+constexpr size_t FORCE_META_BYTES = (size_t)(LIST_STAGE_MAX + 2) * 8;
+constexpr size_t FORCE_INDEX_BYTES = (size_t)(LIST_STAGE_MAX + 4) * 4;
+constexpr size_t FORCE_SMEM = (size_t)BRICK_CAP * 32 + FORCE_LIST_BYTES + FORCE_META_BYTES + FORCE_INDEX_BYTES;
 
 // Slots of each lane's sub-list when Q lanes share a target: sub-list q holds slots
 // [q * sub, (q + 1) * sub) of the target's NBR_CAP slots.
@@ -884,6 +889,8 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
     const float4* s_pos = s_buf;
     const float4* s_vel = s_buf + BRICK_CAP;
     uint16_t* s_lists = reinterpret_cast<uint16_t*>(s_buf + 2 * BRICK_CAP);
+    uint64_t* s_meta = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(s_lists) + FORCE_LIST_BYTES);
+    uint32_t* s_index = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(s_meta) + FORCE_META_BYTES);
     // the next brick's id is fetched while this one is processed
     if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
     for (;;) {
@@ -907,14 +914,21 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
             S.total = acc;
             if (acc <= BRICK_CAP && acc > 0) {
                 const uint32_t lbytes = lists_staged ? ntarg * NBR_CAP * 2 : 0u;
+                // list lengths and permutation entries of the targets, from 16-byte boundaries
+                const uint32_t mbytes = lists_staged ? (((tfirst + ntarg + 1u) & ~1u) - (tfirst & ~1u)) * 8u : 0u;
+                const uint32_t ibytes = lists_staged ? (((tfirst + ntarg + 3u) & ~3u) - (tfirst & ~3u)) * 4u : 0u;
                 fence_proxy_async_smem();
-                mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 32u + lbytes);
+                mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 32u + lbytes + mbytes + ibytes);
                 for (int r = 0; r < R; ++r) {
                     if (!S.rcnt[r]) continue;
                     bulk_g2s(s_buf + S.base[r], spos + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
                     bulk_g2s(s_buf + BRICK_CAP + S.base[r], svel + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
                 }
-                if (lbytes) bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, reinterpret_cast<uint64_t*>(&S.bar));
+                if (lbytes) {
+                    bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, reinterpret_cast<uint64_t*>(&S.bar));
+                    bulk_g2s(s_meta, nbr_meta + (tfirst & ~1u), mbytes, reinterpret_cast<uint64_t*>(&S.bar));
+                    bulk_g2s(s_index, index + (tfirst & ~3u), ibytes, reinterpret_cast<uint64_t*>(&S.bar));
+                }
             }
         }
         __syncthreads();
@@ -956,14 +970,14 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
                 const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
                 if (p == 0) {  // prefetch what the integration needs
-                    o = index[gi];
+                    o = (staged && lists_staged) ? s_index[gi - (tfirst & ~3u)] : index[gi];
                     f_o = force[o];
                     if (FUSED) {
                         v_o = vel[o];
                         p_o = pos[o];
                     }
                 }
-                const uint64_t meta = staged ? nbr_meta[gi] : NBR_SCAN;
+                const uint64_t meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
                 const bool scan = (meta & NBR_SCAN) != 0;
                 if (!scan) {
                     // With four sub-lists lane p takes sub-list p; otherwise the Q sub-lists
