@@ -336,6 +336,32 @@ def extra_adjoint(stream) -> dict:
     return out
 
 
+def extra_bvh(stream) -> dict:
+    """The triangle-mesh BVH build (the reference's other radix-sort user): 1,000,000 small
+    triangles on a jittered 100^3 lattice, shuffled; one build = box, Morton keys, 32-bit sort,
+    nodes, links, leaves, boxes. The CPU restatement of the reference build, single-threaded,
+    on the same mesh beside it."""
+    import torch
+    import oracle
+    from libcl_gb300 import BvhTrimesh
+    from libcl_gb300.scenes import lattice_soup
+    v, idx = lattice_soup(100)
+    dv = torch.from_numpy(v).cuda()
+    di = torch.from_numpy(idx.view(np.int32)).cuda()
+    b = BvhTrimesh()
+    for _ in range(3):
+        b.compute(dv, di, stream)
+    ts = [_time_steps(lambda: b.compute(dv, di, stream), 1, stream) for _ in range(10)]
+    assert b.sync_status() == 0
+    ms = statistics.median(ts)
+    t0 = time.perf_counter()
+    oracle.bvh_build(v, idx, np.zeros(8, np.float32))
+    cpu_s = time.perf_counter() - t0
+    n = idx.size // 3
+    return {"triangles": n, "ms": ms, "triangles_per_s": n / (ms * 1e-3),
+            "cpu_reference_port_ms": cpu_s * 1e3, "cpu_cores": 1}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU port of the reference kernels on a bounded sample."""
     if rank != 0:
@@ -509,7 +535,8 @@ def main(argv=None) -> int:
             del fluid, flush
             torch.cuda.empty_cache()
             result["extras"] = {"batched_256_scenes": extra_batched(stream), "sort_16m": extra_sort(stream),
-                                "two_d": extra_2d(stream), "adjoint": extra_adjoint(stream)}
+                                "two_d": extra_2d(stream), "adjoint": extra_adjoint(stream),
+                                "bvh_1m_triangles": extra_bvh(stream)}
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
     if rank == 0:

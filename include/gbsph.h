@@ -364,6 +364,52 @@ GBSPH_API int gbsph_fluid2d_sync_status(gbsph_fluid2d_t h, void* stream);
 GBSPH_API const char* gbsph_fluid2d_last_error(gbsph_fluid2d_t h);
 
 /* ------------------------------------------------------------------------------------------
+ * Linear BVH over a triangle mesh. Replaces `oclBvhTrimesh` (libCL/geom/oclBvhTrimesh.h:20-84,
+ * libCL/geom/oclBvhTrimesh.cpp:56-178), the reference's other user of the radix sort: global
+ * box of the vertices -> 30-bit Morton key per triangle centroid -> 32-bit sort -> internal
+ * nodes split at the highest differing key bit, linked to the nearer higher-bit neighbour ->
+ * leaves -> boxes. The node layout is the reference's BVHNode (libCL/geom/oclBvhTrimesh.h:
+ * 31-39): nodes [0, n-1) are internal (left/right children), nodes [n-1, 2n-1) are leaves
+ * (left == right == 0, bit = triangle index), internal nodes end with trav = 2. As in the
+ * reference, the global box starts at zero (so it contains the origin) and grows over
+ * builds; it is never reset. Sorted keys that repeat make the reference's linking race; here
+ * the largest claimant of a child slot wins and the build stays deterministic.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbsph_bvh_node {
+    float bbMin[4];
+    float bbMax[4];
+    int32_t left;
+    int32_t right;
+    uint32_t bit;
+    uint32_t trav;
+} gbsph_bvh_node;
+
+typedef struct gbsph_bvh_s* gbsph_bvh_t;
+
+/* oclBvhTrimesh(oclContext&, oclProgram* parent) -- libCL/geom/oclBvhTrimesh.cpp:21-47. */
+GBSPH_API int gbsph_bvh_create(gbsph_bvh_t* out);
+GBSPH_API int gbsph_bvh_destroy(gbsph_bvh_t h);
+/* compute(oclDevice&, oclBuffer& vertex, oclBuffer& index) -- libCL/geom/oclBvhTrimesh.cpp:
+ * 56-143: `vertex` is a device float4[n_vertices], `index` a device uint32[n_indices] (three
+ * per triangle, n_indices / 3 >= 2 triangles). Asynchronous on `stream`. */
+GBSPH_API int gbsph_bvh_compute(gbsph_bvh_t h, const float* vertex, size_t n_vertices, const uint32_t* index,
+                                size_t n_indices, void* stream);
+/* getNodeBuffer / getNodeCount -- libCL/geom/oclBvhTrimesh.cpp:167-175: device nodes
+ * (2n - 1 of them after a build of n triangles). */
+GBSPH_API gbsph_bvh_node* gbsph_bvh_get_node_buffer(gbsph_bvh_t h, size_t* count);
+GBSPH_API size_t gbsph_bvh_get_node_count(gbsph_bvh_t h);
+/* getRootNode -- libCL/geom/oclBvhTrimesh.cpp:162-165 (the reference reads it back after the
+ * build): synchronises `stream` and returns the root's node index. */
+GBSPH_API int gbsph_bvh_get_root_node(gbsph_bvh_t h, uint32_t* root, void* stream);
+/* The accumulated global box (bfAABB, libCL/geom/oclBvhTrimesh.cpp:40): box8 = min xyzw,
+ * max xyzw. Synchronises `stream`. */
+GBSPH_API int gbsph_bvh_get_bounds(gbsph_bvh_t h, float* box8, void* stream);
+/* Synchronises `stream`; reports (and clears) device-side errors: a triangle index outside
+ * the vertex buffer gives GBSPH_ERR_DEVICE_RANGE. */
+GBSPH_API int gbsph_bvh_sync_status(gbsph_bvh_t h, void* stream);
+GBSPH_API const char* gbsph_bvh_last_error(gbsph_bvh_t h);
+
+/* ------------------------------------------------------------------------------------------
  * Adjoint of the 3D step (no counterpart in the reference, which has no derivatives):
  * reverse-mode gradients of a loss on the state after `steps` gbsph_fluid3d_compute() calls
  * with respect to the initial positions and velocities, the gas constant (stiffness) and the

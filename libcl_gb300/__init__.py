@@ -128,6 +128,15 @@ SIGNATURES = {
     "gbsph_fluid2d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
     "gbsph_fluid2d_sync_status": (_I, [_P, _P]),
     "gbsph_fluid2d_last_error": (C.c_char_p, [_P]),
+    "gbsph_bvh_create": (_I, [C.POINTER(_P)]),
+    "gbsph_bvh_destroy": (_I, [_P]),
+    "gbsph_bvh_compute": (_I, [_P, _P, _SZ, _P, _SZ, _P]),
+    "gbsph_bvh_get_node_buffer": (_P, [_P, C.POINTER(_SZ)]),
+    "gbsph_bvh_get_node_count": (_SZ, [_P]),
+    "gbsph_bvh_get_root_node": (_I, [_P, C.POINTER(C.c_uint32), _P]),
+    "gbsph_bvh_get_bounds": (_I, [_P, C.POINTER(C.c_float), _P]),
+    "gbsph_bvh_sync_status": (_I, [_P, _P]),
+    "gbsph_bvh_last_error": (C.c_char_p, [_P]),
     "gbsph_adjoint3d_create": (_I, [C.POINTER(_P), _P, C.c_uint32, C.c_uint32]),
     "gbsph_adjoint3d_destroy": (_I, [_P]),
     "gbsph_adjoint3d_forward": (_I, [_P, _P]),
@@ -409,6 +418,62 @@ class Adjoint3D:
         self._check(self.backward_raw(grad_pos.contiguous(), None if grad_vel is None else grad_vel.contiguous(),
                                       gp0, gv0, gpar, stream))
         return gp0, gv0, gpar
+
+
+class BvhTrimesh:
+    """oclBvhTrimesh (libCL/geom/oclBvhTrimesh.h:20-84): compute(vertex, index) builds the
+    BVH of a triangle mesh; getNodeBuffer / getNodeCount / getRootNode read it. Nodes are
+    48-byte records (bbMin[4], bbMax[4], left, right, bit, trav) returned as an int32 tensor
+    view [count, 12] (use .view(torch.float32) for the boxes)."""
+
+    NODE_WORDS = 12
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_bvh_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_bvh_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_bvh_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_bvh_last_error(self._h).decode())
+
+    def compute_raw(self, vertex, index, stream=None) -> int:
+        return self._lib.gbsph_bvh_compute(self._h, _ptr(vertex), vertex.numel() // 4, _ptr(index), index.numel(),
+                                           _stream(stream))
+
+    def compute(self, vertex, index, stream=None) -> None:
+        """vertex: float32 CUDA tensor [V, 4]; index: int32/uint32 CUDA tensor [3 n]."""
+        self._check(self.compute_raw(vertex, index, stream))
+
+    def getNodeCount(self) -> int:
+        return int(self._lib.gbsph_bvh_get_node_count(self._h))
+
+    def getNodeBuffer(self):
+        import torch
+        count = C.c_size_t()
+        p = self._lib.gbsph_bvh_get_node_buffer(self._h, C.byref(count))
+        return _device_view(p, count.value * self.NODE_WORDS, torch.int32, (count.value, self.NODE_WORDS))
+
+    def getRootNode(self, stream=None) -> int:
+        r = C.c_uint32()
+        self._check(self._lib.gbsph_bvh_get_root_node(self._h, C.byref(r), _stream(stream)))
+        return r.value
+
+    def bounds(self, stream=None):
+        b = (C.c_float * 8)()
+        self._check(self._lib.gbsph_bvh_get_bounds(self._h, b, _stream(stream)))
+        return list(b)
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_bvh_sync_status(self._h, _stream(stream))
 
 
 class Batch3D:

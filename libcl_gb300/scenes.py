@@ -229,3 +229,57 @@ def batched_ensemble(n_scenes: int = 256, seed: int = 5, n_min: int = 4096, n_ma
         first += p.shape[0]
     pos = np.concatenate(pos_l)
     return BatchScenes(shared, descs, pos, np.zeros_like(pos), firsts)
+
+
+def triangle_soup(n: int, seed: int = 21, extent: float = 1.0, size: float = 0.01):
+    """n independent small triangles: centres uniform in [0, extent]^3 (SplitMix64), vertices
+    within +-size of the centre. Returns (vertex float32 [3n, 4] with w = 1, index uint32 [3n])."""
+    rng = SplitMix64(seed)
+    c = rng.uniform(3 * n).reshape(n, 1, 3) * extent
+    d = (rng.uniform(9 * n).reshape(n, 3, 3) * 2.0 - 1.0) * size
+    v = np.ones((3 * n, 4), np.float32)
+    v[:, :3] = (c + d).reshape(3 * n, 3)
+    return v, np.arange(3 * n, dtype=np.uint32)
+
+
+def sphere_mesh(n_lat: int = 64, n_lon: int = 128, radius: float = 0.5, centre=(1.0, 1.0, 1.0)):
+    """A UV sphere: (n_lat - 1) * n_lon + 2 shared vertices, 2 * n_lon * (n_lat - 1) triangles.
+    Returns (vertex float32 [V, 4] with w = 0, index uint32 [3T])."""
+    verts = [(0.0, 0.0, radius)]
+    for i in range(1, n_lat):
+        th = np.pi * i / n_lat
+        for j in range(n_lon):
+            ph = 2.0 * np.pi * j / n_lon
+            verts.append((radius * np.sin(th) * np.cos(ph), radius * np.sin(th) * np.sin(ph), radius * np.cos(th)))
+    verts.append((0.0, 0.0, -radius))
+    v = np.zeros((len(verts), 4), np.float32)
+    v[:, :3] = np.asarray(verts) + np.asarray(centre)
+    tris = []
+    for j in range(n_lon):  # north cap
+        tris.append((0, 1 + j, 1 + (j + 1) % n_lon))
+    for i in range(n_lat - 2):
+        a, b = 1 + i * n_lon, 1 + (i + 1) * n_lon
+        for j in range(n_lon):
+            jn = (j + 1) % n_lon
+            tris.append((a + j, b + j, b + jn))
+            tris.append((a + j, b + jn, a + jn))
+    last, south = 1 + (n_lat - 2) * n_lon, len(verts) - 1
+    for j in range(n_lon):  # south cap
+        tris.append((last + j, south, last + (j + 1) % n_lon))
+    return v, np.asarray(tris, np.uint32).ravel()
+
+
+def lattice_soup(k: int = 100, seed: int = 22, size: float = 0.002):
+    """k^3 small triangles centred on a jittered k x k x k lattice in [0.05, 1.05]^3 (one per
+    lattice cell, so with k <= 1024 their Morton keys are distinct), shuffled. Returns (vertex
+    float32 [3 k^3, 4] with w = 1, index uint32 [3 k^3])."""
+    rng = SplitMix64(seed)
+    n = k ** 3
+    iz, iy, ix = np.meshgrid(np.arange(k), np.arange(k), np.arange(k), indexing="ij")
+    c = np.stack([ix.ravel(), iy.ravel(), iz.ravel()], axis=1).astype(np.float64)
+    c = 0.05 + (c + 0.25 + 0.5 * rng.uniform(3 * n).reshape(n, 3)) / k
+    c = c[np.argsort(rng.next_u64(n), kind="stable")]
+    d = (rng.uniform(9 * n).reshape(n, 3, 3) * 2.0 - 1.0) * size
+    v = np.ones((3 * n, 4), np.float32)
+    v[:, :3] = (c[:, None, :] + d).reshape(3 * n, 3)
+    return v, np.arange(3 * n, dtype=np.uint32)

@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
             "orc_run_f64": (C.c_int, [P, P, P, U, P, U]),
             "orc_adjoint_f64": (C.c_int, [P, P, P, U, P, U, U, P, P, P, P, P]),
             "orc_adjoint_states_f64": (C.c_int, [P, P, P, U, P, U, P, P, P, P, P]),
+            "orc_bvh_build": (C.c_int, [P, U, P, U, P, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -279,3 +280,23 @@ def adjoint_states_f64(states_pos, states_vel, force0, params, gpos, gvel=None):
                                       None if gvel is None else _p(gvel), _p(gp0), _p(gv0), _p(gpar))
     assert rc == 0, rc
     return gp0, gv0, float(gpar[0]), float(gpar[1])
+
+
+BVH_NODE_DTYPE = np.dtype([("bbMin", np.float32, 4), ("bbMax", np.float32, 4), ("left", np.int32),
+                           ("right", np.int32), ("bit", np.uint32), ("trav", np.uint32)])
+
+
+def bvh_build(vertex: np.ndarray, index: np.ndarray, box: np.ndarray, root: int = 0):
+    """The reference's BVH build (oclBvhTrimesh::compute) on host arrays: vertex float32
+    [V, 4], index uint32 [3 n], box float32 [8] updated in place (the persistent global box).
+    Returns (nodes [2n - 1] structured array, root, sorted keys, sorted triangle ids)."""
+    vertex = np.ascontiguousarray(vertex, np.float32)
+    index = np.ascontiguousarray(index, np.uint32)
+    n = index.size // 3
+    nodes = np.zeros(2 * n - 1, BVH_NODE_DTYPE)
+    r = np.array([root], np.uint32)
+    sk = np.empty(n, np.uint32)
+    sv = np.empty(n, np.uint32)
+    rc = lib().orc_bvh_build(_p(vertex), vertex.shape[0], _p(index), n, _p(box), _p(nodes), _p(r), _p(sk), _p(sv))
+    assert rc == 0, rc
+    return nodes, int(r[0]), sk, sv

@@ -1,0 +1,185 @@
+// oraclebvh.cpp -- CPU restatement of the reference's triangle-mesh BVH build.
+//
+// TEST INFRASTRUCTURE ONLY, like oracle3d.cpp: nothing in the product links or calls it.
+// It follows oclBvhTrimesh::compute (libCL/geom/oclBvhTrimesh.cpp:56-143) and the kernels of
+// libCL/geom/oclBvhTrimesh.cl step by step, one work-item at a time, with the reference's own
+// algorithms (linear neighbour scans, per-triangle root-to-leaf descents with visit flags).
+// OpenCL's float min(x, y) is y < x ? y : x and max(x, y) is x < y ? y : x; float-to-uint
+// conversion truncates. Parity status: unpinned against executed reference output (no OpenCL
+// device here); pinned by construction against the .cl source and by structural checks.
+
+#include <algorithm>
+#include <cfloat>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/gbsph.h"
+
+namespace {
+
+inline float clmin(float x, float y) { return y < x ? y : x; }
+inline float clmax(float x, float y) { return x < y ? y : x; }
+
+// "code", libCL/geom/oclBvhTrimesh.cl:82-89
+uint32_t code(uint32_t x) {
+    x = (x | (x << 16)) & 0x030000FF;
+    x = (x | (x << 8)) & 0x0300F00F;
+    x = (x | (x << 4)) & 0x030C30C3;
+    x = (x | (x << 2)) & 0x09249249;
+    return x;
+}
+
+// float -> uint as the implicit OpenCL C conversion (truncation); NaN and negatives -> 0,
+// which is what the GPU conversion gives.
+uint32_t to_uint(float f) {
+    if (!(f > 0.0f)) return 0;
+    if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+    return (uint32_t)f;
+}
+
+void init_node(gbsph_bvh_node& nd, int32_t l, int32_t r, uint32_t bit) {
+    nd.bbMin[0] = nd.bbMin[1] = nd.bbMin[2] = FLT_MAX;
+    nd.bbMin[3] = 0.0f;
+    nd.bbMax[0] = nd.bbMax[1] = nd.bbMax[2] = -FLT_MAX;
+    nd.bbMax[3] = 0.0f;
+    nd.left = l;
+    nd.right = r;
+    nd.bit = bit;
+    nd.trav = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// One build. vertex: float4[nv]; index: uint32[3 n]; box: float[8] in/out (min xyzw, max
+// xyzw; the reference's bfAABB, zero before the first build); nodes: [2n - 1]; root: in/out
+// (the reference keeps mRootNode across builds). Returns 0, or -1 for n < 2.
+int orc_bvh_build(const float* vertex, uint32_t nv, const uint32_t* index, uint32_t n, float* box,
+                  gbsph_bvh_node* nodes, uint32_t* root, uint32_t* sorted_keys, uint32_t* sorted_vals) {
+    if (n < 2) return -1;
+    // clAABB (libCL/geom/oclBvhTrimesh.cl:33-76): min / max of every vertex, all four lanes,
+    // into the persistent box
+    for (uint32_t i = 0; i < nv; i++)
+        for (int c = 0; c < 4; c++) {
+            box[c] = clmin(box[c], vertex[4 * i + c]);
+            box[4 + c] = clmax(box[4 + c], vertex[4 * i + c]);
+        }
+    // clMorton (:91-103)
+    std::vector<uint32_t> key(n), val(n);
+    for (uint32_t g = 0; g < n; g++) {
+        const float* v0 = vertex + 4 * (size_t)index[3 * g];
+        const float* v1 = vertex + 4 * (size_t)index[3 * g + 1];
+        const float* v2 = vertex + 4 * (size_t)index[3 * g + 2];
+        uint32_t k = 0;
+        for (int c = 0; c < 3; c++) {
+            const float cen = ((v0[c] + v1[c]) + v2[c]) / 3.0f;
+            const float t = (cen - box[c]) / (box[4 + c] - box[c]);
+            k |= code(to_uint(t * (float)0x3FF)) << c;
+        }
+        key[g] = k;
+        val[g] = g;
+    }
+    // oclRadixSort on bits [0, 32): a stable sort
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    std::vector<uint32_t> sk(n), sv(n);
+    for (uint32_t i = 0; i < n; i++) {
+        sk[i] = key[order[i]];
+        sv[i] = val[order[i]];
+    }
+    const uint32_t m = n - 1;  // internal nodes
+    // clCreateNodes (:119-143)
+    for (uint32_t i = 0; i < m; i++) {
+        uint32_t bit = 0;
+        for (int b = 29; b >= 0; b--)
+            if (((sk[i] >> b) & 1u) != ((sk[i + 1] >> b) & 1u)) {
+                bit = (uint32_t)b;
+                break;
+            }
+        init_node(nodes[i], -1, -1, bit);
+    }
+    // clLinkNodes (:145-199)
+    for (uint32_t g = 0; g < m; g++) {
+        const uint32_t bit = nodes[g].bit;
+        int left = -1, right = -1;
+        for (int i = (int)g - 1; i >= 0; i--)
+            if (nodes[i].bit > bit) {
+                left = i;
+                break;
+            }
+        for (uint32_t i = g + 1; i < m; i++)
+            if (nodes[i].bit > bit) {
+                right = (int)i;
+                break;
+            }
+        if (left != -1 || right != -1) {
+            if (right == -1) nodes[left].right = (int32_t)g;
+            else if (left == -1) nodes[right].left = (int32_t)g;
+            else if (nodes[left].bit < nodes[right].bit) nodes[left].right = (int32_t)g;
+            else nodes[right].left = (int32_t)g;
+        } else {
+            *root = g;
+        }
+    }
+    // clCreateLeaves (:201-234)
+    const uint32_t ls = n - 1;
+    for (uint32_t g = 0; g < n; g++) {
+        init_node(nodes[ls + g], 0, 0, sv[g]);
+        if (g == 0) {
+            nodes[0].left = (int32_t)(ls + g);
+            continue;
+        }
+        if (g == ls) {
+            nodes[ls - 1].right = (int32_t)(ls + g);
+            continue;
+        }
+        if (nodes[g].left == -1) nodes[g].left = (int32_t)(g + ls);
+        else if (nodes[g - 1].right == -1) nodes[g - 1].right = (int32_t)(g + ls);
+    }
+    // clComputeAABBs (:236-298): per triangle, descend by node index, box the leaf, then
+    // climb: the first visitor of a node marks it and stops, the second computes its box
+    for (uint32_t g = 0; g < n; g++) {
+        std::vector<uint32_t> stack;
+        stack.push_back(*root);
+        for (;;) {
+            gbsph_bvh_node& nd = nodes[stack.back()];
+            if (nd.left == nd.right) {
+                const uint32_t tri = nd.bit;
+                float mn[4] = {FLT_MAX, FLT_MAX, FLT_MAX, 0.0f}, mx[4] = {-FLT_MAX, -FLT_MAX, -FLT_MAX, 0.0f};
+                for (int k = 0; k < 3; k++)
+                    for (int c = 0; c < 4; c++) {
+                        const float v = vertex[4 * (size_t)index[3 * tri + k] + c];
+                        mn[c] = clmin(mn[c], v);
+                        mx[c] = clmax(mx[c], v);
+                    }
+                std::memcpy(nd.bbMin, mn, 16);
+                std::memcpy(nd.bbMax, mx, 16);
+                break;
+            }
+            stack.push_back(stack.back() >= g ? (uint32_t)nd.left : (uint32_t)nd.right);
+            if (stack.size() > 2 * (size_t)n) return -2;  // not a tree
+        }
+        size_t top = stack.size() - 1;
+        while (top--) {
+            gbsph_bvh_node& nd = nodes[stack[top]];
+            if (nd.trav == 0) {
+                nd.trav = 2;
+                break;
+            }
+            const gbsph_bvh_node& l = nodes[nd.left];
+            const gbsph_bvh_node& r = nodes[nd.right];
+            for (int c = 0; c < 4; c++) {
+                nd.bbMin[c] = clmin(l.bbMin[c], r.bbMin[c]);
+                nd.bbMax[c] = clmax(l.bbMax[c], r.bbMax[c]);
+            }
+        }
+    }
+    if (sorted_keys) std::memcpy(sorted_keys, sk.data(), 4 * (size_t)n);
+    if (sorted_vals) std::memcpy(sorted_vals, sv.data(), 4 * (size_t)n);
+    return 0;
+}
+
+}  // extern "C"

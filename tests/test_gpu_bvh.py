@@ -1,0 +1,95 @@
+"""GPU parity of the triangle-mesh BVH (gbsph_bvh_*) against the oracle's restatement of
+oclBvhTrimesh: every node (boxes, children, split bit or triangle, visit flag), the root and
+the accumulated global box bit-exact."""
+import numpy as np
+import pytest
+
+import oracle
+from libcl_gb300 import ERR_ARGUMENT, ERR_DEVICE_RANGE, BvhTrimesh
+from libcl_gb300.scenes import lattice_soup, sphere_mesh, triangle_soup
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_nodes(b):
+    return b.getNodeBuffer().cpu().numpy().view(oracle.BVH_NODE_DTYPE).ravel()
+
+
+def build_both(b, v, idx, box, root):
+    import torch
+    b.compute(torch.from_numpy(v).cuda(), torch.from_numpy(idx.view(np.int32)).cuda())
+    assert b.sync_status() == 0
+    nodes, root, sk, sv = oracle.bvh_build(v, idx, box, root)
+    return nodes, root, sk
+
+
+def assert_same(g, o):
+    for f in ("left", "right", "bit", "trav"):
+        np.testing.assert_array_equal(g[f], o[f], err_msg=f)
+    for f in ("bbMin", "bbMax"):
+        np.testing.assert_array_equal(g[f].view(np.uint32), o[f].view(np.uint32), err_msg=f)
+
+
+@pytest.mark.parametrize("mesh", ["soup_20k", "sphere", "lattice_1m"])
+def test_bvh_bit_exact(cuda, mesh):
+    if mesh == "soup_20k":
+        v, idx = triangle_soup(20000)
+    elif mesh == "sphere":
+        v, idx = sphere_mesh(24, 48)
+    else:
+        v, idx = lattice_soup(100)
+    b = BvhTrimesh()
+    box = np.zeros(8, np.float32)
+    o, root, sk = build_both(b, v, idx, box, 0)
+    if len(np.unique(sk)) != sk.size:
+        pytest.skip("repeated Morton keys (the reference's linking races on them)")
+    assert b.getNodeCount() == 2 * (idx.size // 3) - 1
+    assert b.getRootNode() == root
+    assert_same(gpu_nodes(b), o)
+    np.testing.assert_array_equal(np.asarray(b.bounds(), np.float32).view(np.uint32), box.view(np.uint32))
+
+
+def test_bvh_rebuild_keeps_growing_box(cuda):
+    """Two builds on one handle: the second mesh is smaller and elsewhere; the global box
+    only grows and the nodes follow it, as in the reference."""
+    b = BvhTrimesh()
+    box = np.zeros(8, np.float32)
+    v1, i1 = triangle_soup(5000, seed=3, extent=2.0)
+    o, root, _ = build_both(b, v1, i1, box, 0)
+    v2, i2 = sphere_mesh(16, 32, radius=0.3, centre=(-1.0, 0.5, 0.5))
+    o, root, sk = build_both(b, v2, i2, box, root)
+    assert len(np.unique(sk)) == sk.size
+    assert b.getRootNode() == root
+    assert_same(gpu_nodes(b), o)
+    np.testing.assert_array_equal(np.asarray(b.bounds(), np.float32), box)
+
+
+def test_bvh_errors(cuda):
+    import torch
+    b = BvhTrimesh()
+    v = torch.zeros(4, 4, device="cuda")
+    with pytest.raises(Exception) as e:
+        b.compute(v, torch.zeros(3, dtype=torch.int32, device="cuda"))  # one triangle
+    assert e.value.status == ERR_ARGUMENT
+    with pytest.raises(Exception) as e:
+        b.compute(v, torch.zeros(7, dtype=torch.int32, device="cuda"))
+    assert e.value.status == ERR_ARGUMENT
+    b.compute(v, torch.tensor([0, 1, 2, 1, 2, 9], dtype=torch.int32, device="cuda"))  # vertex 9 does not exist
+    assert b.sync_status() == ERR_DEVICE_RANGE
+
+
+def test_bvh_repeated_keys_links_as_a_sequential_run(cuda):
+    """A finer sphere has triangles near the poles with equal Morton keys. The reference's
+    linking then races (several nodes claim one child slot); here the last claimant in
+    work-item order wins, as in the oracle's sequential run: children, split bits, leaves and
+    root match. (Boxes are not compared: the reference's per-triangle descent is not defined
+    on the resulting graph.)"""
+    v, idx = sphere_mesh(64, 128)
+    b = BvhTrimesh()
+    box = np.zeros(8, np.float32)
+    o, root, sk = build_both(b, v, idx, box, 0)
+    assert len(np.unique(sk)) < sk.size
+    g = gpu_nodes(b)
+    for f in ("left", "right", "bit"):
+        np.testing.assert_array_equal(g[f], o[f], err_msg=f)
+    assert b.getRootNode() == root

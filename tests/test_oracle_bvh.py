@@ -1,0 +1,55 @@
+"""The oracle's restatement of the reference's BVH build (CPU only): the tree it produces is
+a binary tree over all triangles whose boxes nest, and its global box behaves as the
+reference's (starts at zero, only grows)."""
+import numpy as np
+import pytest
+
+import oracle
+from libcl_gb300.scenes import sphere_mesh, triangle_soup
+
+
+def check_tree(nodes, root, vertex, index):
+    n = (nodes.size + 1) // 2
+    seen = np.zeros(nodes.size, np.int32)
+    stack = [root]
+    leaves = []
+    while stack:
+        i = stack.pop()
+        seen[i] += 1
+        nd = nodes[i]
+        if nd["left"] == nd["right"]:
+            assert i >= n - 1
+            leaves.append(int(nd["bit"]))
+            tri = vertex[index[3 * nd["bit"]:3 * nd["bit"] + 3]]
+            np.testing.assert_array_equal(nd["bbMin"][:3], tri[:, :3].min(axis=0))
+            np.testing.assert_array_equal(nd["bbMax"][:3], tri[:, :3].max(axis=0))
+            continue
+        assert i < n - 1 and nd["trav"] == 2
+        for c in (nd["left"], nd["right"]):
+            assert np.all(nodes[c]["bbMin"] >= nd["bbMin"]) and np.all(nodes[c]["bbMax"] <= nd["bbMax"])
+            stack.append(int(c))
+    assert np.all(seen == 1), "every node reached exactly once"
+    assert sorted(leaves) == list(range(n))
+
+
+@pytest.mark.parametrize("mesh", ["soup", "sphere"])
+def test_bvh_oracle_builds_a_tree(mesh):
+    v, idx = triangle_soup(3000) if mesh == "soup" else sphere_mesh(24, 48)
+    box = np.zeros(8, np.float32)
+    nodes, root, sk, sv = oracle.bvh_build(v, idx, box)
+    assert np.all(sk[1:] >= sk[:-1])
+    assert len(np.unique(sk)) == sk.size, "this mesh has distinct Morton keys"
+    check_tree(nodes, root, v, idx)
+    # the global box contains the origin (it starts at zero) and every vertex
+    assert np.all(box[:3] <= np.minimum(0, v[:, :3].min(axis=0))) and np.all(box[4:7] >= v[:, :3].max(axis=0))
+
+
+def test_bvh_oracle_box_only_grows():
+    v, idx = triangle_soup(500, extent=2.0)
+    box = np.zeros(8, np.float32)
+    oracle.bvh_build(v, idx, box)
+    first = box.copy()
+    v2 = v.copy()
+    v2[:, :3] *= 0.25
+    oracle.bvh_build(v2, idx, box)
+    np.testing.assert_array_equal(box, first)  # a smaller mesh does not shrink it
