@@ -408,6 +408,17 @@ GBSPH_API int gbsph_bvh_get_bounds(gbsph_bvh_t h, float* box8, void* stream);
  * the vertex buffer gives GBSPH_ERR_DEVICE_RANGE. */
 GBSPH_API int gbsph_bvh_sync_status(gbsph_bvh_t h, void* stream);
 GBSPH_API const char* gbsph_bvh_last_error(gbsph_bvh_t h);
+/* clCollideBVH (libCL/phys/oclFluid3D.cl:365-550; the reference's step does not enqueue it, a
+ * caller adds it, e.g. from the integrate hook): per particle, a breadth-first walk of the
+ * last built BVH (256-entry circular queue, boxes tested along the velocity ray) stops at the
+ * first triangle the particle's next displacement crosses within particleRadius; that
+ * particle's position, velocity and force (device float4[n_particles]) are then updated as
+ * the reference does. Uses deltaTime, particleRadius, pressureConstant, density, cellSize and
+ * mass of `params`; `vertex` / `index` are the mesh the BVH was built from. Reads the root
+ * back (synchronises `stream` once), then runs asynchronously. */
+GBSPH_API int gbsph_bvh_collide(gbsph_bvh_t h, const gbsph_fluid3d_params* params, float* position,
+                                float* velocity, float* force, size_t n_particles, const float* vertex,
+                                size_t n_vertices, const uint32_t* index, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Adjoint of the 3D step (no counterpart in the reference, which has no derivatives):

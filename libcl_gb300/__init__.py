@@ -137,6 +137,7 @@ SIGNATURES = {
     "gbsph_bvh_get_bounds": (_I, [_P, C.POINTER(C.c_float), _P]),
     "gbsph_bvh_sync_status": (_I, [_P, _P]),
     "gbsph_bvh_last_error": (C.c_char_p, [_P]),
+    "gbsph_bvh_collide": (_I, [_P, C.POINTER(Fluid3DParams), _P, _P, _P, _SZ, _P, _SZ, _P, _P]),
     "gbsph_adjoint3d_create": (_I, [C.POINTER(_P), _P, C.c_uint32, C.c_uint32]),
     "gbsph_adjoint3d_destroy": (_I, [_P]),
     "gbsph_adjoint3d_forward": (_I, [_P, _P]),
@@ -474,6 +475,13 @@ class BvhTrimesh:
 
     def sync_status(self, stream=None) -> int:
         return self._lib.gbsph_bvh_sync_status(self._h, _stream(stream))
+
+    def collide(self, params: Fluid3DParams, position, velocity, force, vertex, index, stream=None) -> None:
+        """clCollideBVH on particle float4 tensors [N, 4] (updated in place) against the mesh
+        (vertex [V, 4], index [3 n]) this BVH was last built from."""
+        self._check(self._lib.gbsph_bvh_collide(self._h, C.byref(params), _ptr(position), _ptr(velocity), _ptr(force),
+                                                position.numel() // 4, _ptr(vertex), vertex.numel() // 4, _ptr(index),
+                                                _stream(stream)))
 
 
 class Batch3D:

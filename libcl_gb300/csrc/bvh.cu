@@ -457,3 +457,183 @@ GBSPH_API int gbsph_bvh_sync_status(gbsph_bvh_t h, void* stream) {
 GBSPH_API const char* gbsph_bvh_last_error(gbsph_bvh_t h) { return h ? h->last_error.c_str() : "null handle"; }
 
 }  // extern "C"
+
+// ---- particle-vs-mesh collision -------------------------------------------------------------
+// clCollideBVH (libCL/phys/oclFluid3D.cl:365-550), one work-item per particle, restated with
+// round-to-nearest intrinsics (no contraction) so that it matches the CPU restatement bit for
+// bit. OpenCL's implementation-defined helpers are fixed as: dot(a, b) = ((ax bx + ay by) +
+// az bz) + aw bw; length / fast_length(a) = sqrt(dot(a, a)); normalize(a) = a / length(a)
+// per lane; cross() of float4 has w = 0. The traversal keeps the reference's breadth-first
+// order with its 256-entry circular queue, so the first colliding triangle is the same.
+
+namespace {
+
+struct F4 {
+    float x, y, z, w;
+};
+__device__ __forceinline__ F4 f4(float4 a) { return {a.x, a.y, a.z, a.w}; }
+__device__ __forceinline__ F4 add(F4 a, F4 b) {
+    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w)};
+}
+__device__ __forceinline__ F4 sub(F4 a, F4 b) {
+    return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w)};
+}
+__device__ __forceinline__ F4 mul(F4 a, float s) {
+    return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s), __fmul_rn(a.w, s)};
+}
+__device__ __forceinline__ F4 mulv(F4 a, F4 b) {
+    return {__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z), __fmul_rn(a.w, b.w)};
+}
+__device__ __forceinline__ F4 divs(F4 a, float s) {
+    return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s), __fdiv_rn(a.w, s)};
+}
+__device__ __forceinline__ float dot(F4 a, F4 b) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z)),
+                     __fmul_rn(a.w, b.w));
+}
+__device__ __forceinline__ float len(F4 a) { return __fsqrt_rn(dot(a, a)); }
+__device__ __forceinline__ F4 normalize(F4 a) { return divs(a, len(a)); }
+__device__ __forceinline__ F4 cross(F4 p, F4 q) {
+    return {__fsub_rn(__fmul_rn(p.y, q.z), __fmul_rn(p.z, q.y)), __fsub_rn(__fmul_rn(p.z, q.x), __fmul_rn(p.x, q.z)),
+            __fsub_rn(__fmul_rn(p.x, q.y), __fmul_rn(p.y, q.x)), 0.0f};
+}
+
+struct CollideParams {
+    float dt, radius, pconst, density, h, mass;
+};
+
+// collideTriangle (libCL/phys/oclFluid3D.cl:380-459); `tri` is the first index slot.
+__device__ bool collide_triangle(uint32_t tri, const uint32_t* __restrict__ index, const float4* __restrict__ vertex,
+                                 uint32_t nv, F4& pos, F4& vel, F4& force, const CollideParams& P) {
+    F4 V0 = f4(vertex[min(index[tri], nv - 1)]), V1 = f4(vertex[min(index[tri + 1], nv - 1)]),
+       V2 = f4(vertex[min(index[tri + 2], nv - 1)]);
+    V0.w = V1.w = V2.w = 0.0f;
+    pos.w = 0.0f;
+    const F4 u = sub(V1, V0), v = sub(V2, V0);
+    F4 n = cross(u, v);
+    if (dot(n, n) == 0.0f) return false;
+    const F4 w0 = sub(pos, V0);
+    const F4 disp = mul(vel, P.dt);
+    const float a = dot(n, w0);
+    if (a < 0.0f) return false;
+    const float b = dot(n, disp);
+    if (fabsf(b) < 0.000001f) return false;
+    const float r = __fdiv_rn(-a, b);
+    if (r < 0.0f) return false;
+    const F4 I = add(pos, mul(disp, r));
+    const float uu = dot(u, u), uv = dot(u, v), vv = dot(v, v);
+    const F4 w = sub(I, V0);
+    const float wu = dot(w, u), wv = dot(w, v);
+    const float D = __fsub_rn(__fmul_rn(uv, uv), __fmul_rn(uu, vv));
+    const float s = __fdiv_rn(__fsub_rn(__fmul_rn(uv, wv), __fmul_rn(vv, wu)), D);
+    if (s < 0.0f || s > 1.0f) return false;
+    const float t = __fdiv_rn(__fsub_rn(__fmul_rn(uv, wu), __fmul_rn(uu, wv)), D);
+    if (t < 0.0f || __fadd_rn(s, t) > 1.0f) return false;
+    n = normalize(n);
+    const F4 Vc = sub(add(pos, disp), V0);
+    const float dist = dot(Vc, n);
+    const float depth = __fsub_rn(P.radius, dist);
+    if (depth > 0.0f) {
+        const F4 dPos = mul(mul(normalize(disp), dot(n, disp)), depth);
+        const F4 dTan = sub(vel, mul(n, dot(n, vel)));
+        force = add(force, divs(dTan, P.dt));
+        const float hd = __fsub_rn(P.h, dist);
+        force = add(force, mul(mul(mul(mul(n, hd), hd), __fdiv_rn(P.pconst, P.density)), P.mass));
+        pos = add(pos, dPos);
+        vel = {0.0f, 0.0f, 0.0f, 0.0f};
+        return true;
+    }
+    return false;
+}
+
+// intersectBox + collideAABB (libCL/phys/oclFluid3D.cl:462-498).
+__device__ bool collide_box(const gbsph_bvh_node& nd, F4 pos, F4 vel, float radius) {
+    const F4 nr = normalize(vel);
+    const F4 inv = {__fdiv_rn(1.0f, nr.x), __fdiv_rn(1.0f, nr.y), __fdiv_rn(1.0f, nr.z), __fdiv_rn(1.0f, nr.w)};
+    const F4 bmin = {nd.bbMin[0], nd.bbMin[1], nd.bbMin[2], nd.bbMin[3]};
+    const F4 bmax = {nd.bbMax[0], nd.bbMax[1], nd.bbMax[2], nd.bbMax[3]};
+    const F4 tbot = mulv(inv, sub(bmin, pos)), ttop = mulv(inv, sub(bmax, pos));
+    const float tminx = cl_min(ttop.x, tbot.x), tminy = cl_min(ttop.y, tbot.y), tminz = cl_min(ttop.z, tbot.z);
+    const float tmaxx = cl_max(ttop.x, tbot.x), tmaxy = cl_max(ttop.y, tbot.y), tmaxz = cl_max(ttop.z, tbot.z);
+    const float tnear = cl_max(cl_max(tminx, tminy), cl_max(tminx, tminz));
+    const float tfar = cl_min(cl_min(tmaxx, tmaxy), cl_min(tmaxx, tmaxz));
+    if (!(tfar > tnear)) return false;
+    return tnear < cl_max(radius, len(vel));
+}
+
+constexpr uint32_t QUEUE_SIZE = 256;
+
+__global__ void __launch_bounds__(BVH_THREADS) k_collide_bvh(float4* __restrict__ force, float4* __restrict__ position,
+                                                             float4* __restrict__ velocity, uint32_t np,
+                                                             CollideParams P, const gbsph_bvh_node* __restrict__ bvh,
+                                                             uint32_t root, uint32_t n_nodes,
+                                                             const uint32_t* __restrict__ index,
+                                                             const float4* __restrict__ vertex, uint32_t nv,
+                                                             uint32_t* err) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    F4 pos = f4(position[p]), vel = f4(velocity[p]), frc = f4(force[p]);
+    uint32_t queue[QUEUE_SIZE];
+    uint32_t head = 0, tail = 1;
+    queue[0] = root;
+    uint32_t steps = 0;
+    while (head != tail) {
+        const uint32_t it = queue[head];
+        head = (head + 1) % QUEUE_SIZE;
+        if (it >= n_nodes || ++steps > 4u * n_nodes + 4u) {  // not a tree: report and stop
+            atomicOr(err, DEV_ERR_KEY_RANGE);
+            return;
+        }
+        const uint32_t l = (uint32_t)bvh[it].left, r = (uint32_t)bvh[it].right;
+        if (l == r) {
+            if (collide_triangle(bvh[it].bit * 3u, index, vertex, nv, pos, vel, frc, P)) {
+                position[p] = make_float4(pos.x, pos.y, pos.z, pos.w);
+                velocity[p] = make_float4(vel.x, vel.y, vel.z, vel.w);
+                force[p] = make_float4(frc.x, frc.y, frc.z, frc.w);
+                break;
+            }
+        } else {
+            if (l < n_nodes && collide_box(bvh[l], pos, vel, P.radius)) {
+                queue[tail] = l;
+                tail = (tail + 1) % QUEUE_SIZE;
+            }
+            if (r < n_nodes && collide_box(bvh[r], pos, vel, P.radius)) {
+                queue[tail] = r;
+                tail = (tail + 1) % QUEUE_SIZE;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" GBSPH_API int gbsph_bvh_collide(gbsph_bvh_t h, const gbsph_fluid3d_params* params, float* position,
+                                           float* velocity, float* force, size_t n_particles, const float* vertex,
+                                           size_t n_vertices, const uint32_t* index, void* stream) {
+    if (!h || !params) return GBSPH_ERR_ARGUMENT;
+    if (!position || !velocity || !force || !vertex || !index)
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null buffer");
+    if (h->n == 0) return fail(&h->last_error, GBSPH_ERR_STATE, "collide before a BVH was built");
+    if (n_particles == 0) return GBSPH_OK;
+    if (n_particles > 0xFFFFFFFFull || n_vertices == 0 || n_vertices > 0xFFFFFFFFull)
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "bad particle or vertex count");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    uint32_t root = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(&root, h->root, 4, cudaMemcpyDeviceToHost, s));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize(s));
+    CollideParams P;
+    P.dt = params->deltaTime;
+    P.radius = params->particleRadius;
+    P.pconst = params->pressureConstant;
+    P.density = params->density;
+    P.h = params->cellSize;
+    P.mass = params->mass;
+    const uint32_t np = (uint32_t)n_particles;
+    k_collide_bvh<<<grid(np), BVH_THREADS, 0, s>>>(reinterpret_cast<float4*>(force), reinterpret_cast<float4*>(position),
+                                                   reinterpret_cast<float4*>(velocity), np, P, h->node, root,
+                                                   2 * h->n - 1, index, reinterpret_cast<const float4*>(vertex),
+                                                   (uint32_t)n_vertices, h->err);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}

@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
             "orc_adjoint_f64": (C.c_int, [P, P, P, U, P, U, U, P, P, P, P, P]),
             "orc_adjoint_states_f64": (C.c_int, [P, P, P, U, P, U, P, P, P, P, P]),
             "orc_bvh_build": (C.c_int, [P, U, P, U, P, P, P, P, P]),
+            "orc_bvh_collide": (None, [P, P, P, P, U, P, U, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -300,3 +301,9 @@ def bvh_build(vertex: np.ndarray, index: np.ndarray, box: np.ndarray, root: int 
     rc = lib().orc_bvh_build(_p(vertex), vertex.shape[0], _p(index), n, _p(box), _p(nodes), _p(r), _p(sk), _p(sv))
     assert rc == 0, rc
     return nodes, int(r[0]), sk, sv
+
+
+def bvh_collide(params, position, velocity, force, nodes, root, index, vertex) -> None:
+    """clCollideBVH on host float32 [N, 4] arrays (updated in place)."""
+    lib().orc_bvh_collide(_pp(params), _p(position), _p(velocity), _p(force), position.shape[0], _p(nodes), root,
+                          _p(np.ascontiguousarray(index, np.uint32)), _p(np.ascontiguousarray(vertex, np.float32)))

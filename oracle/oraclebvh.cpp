@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -180,6 +181,126 @@ int orc_bvh_build(const float* vertex, uint32_t nv, const uint32_t* index, uint3
     if (sorted_keys) std::memcpy(sorted_keys, sk.data(), 4 * (size_t)n);
     if (sorted_vals) std::memcpy(sorted_vals, sv.data(), 4 * (size_t)n);
     return 0;
+}
+
+}  // extern "C"
+
+// ---- clCollideBVH (libCL/phys/oclFluid3D.cl:365-550), one particle at a time ---------------
+// Helpers fixed as in the library: dot = ((ax bx + ay by) + az bz) + aw bw, length =
+// sqrt(dot(a, a)), normalize(a) = a / length(a) per lane, cross() with w = 0.
+namespace {
+
+struct F4 {
+    float x, y, z, w;
+};
+F4 add(F4 a, F4 b) { return {a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+F4 sub(F4 a, F4 b) { return {a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w}; }
+F4 mul(F4 a, float s) { return {a.x * s, a.y * s, a.z * s, a.w * s}; }
+F4 mulv(F4 a, F4 b) { return {a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w}; }
+F4 divs(F4 a, float s) { return {a.x / s, a.y / s, a.z / s, a.w / s}; }
+float dot(F4 a, F4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+float len(F4 a) { return std::sqrt(dot(a, a)); }
+F4 normalize(F4 a) { return divs(a, len(a)); }
+F4 cross(F4 p, F4 q) { return {p.y * q.z - p.z * q.y, p.z * q.x - p.x * q.z, p.x * q.y - p.y * q.x, 0.0f}; }
+F4 load(const float* v, size_t i) { return {v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]}; }
+void store(float* v, size_t i, F4 a) {
+    v[4 * i] = a.x;
+    v[4 * i + 1] = a.y;
+    v[4 * i + 2] = a.z;
+    v[4 * i + 3] = a.w;
+}
+
+bool collide_triangle(uint32_t tri, const uint32_t* index, const float* vertex, F4& pos, F4& vel, F4& force,
+                      const gbsph_fluid3d_params& P) {
+    F4 V0 = load(vertex, index[tri]), V1 = load(vertex, index[tri + 1]), V2 = load(vertex, index[tri + 2]);
+    V0.w = V1.w = V2.w = 0.0f;
+    pos.w = 0.0f;
+    const F4 u = sub(V1, V0), v = sub(V2, V0);
+    F4 n = cross(u, v);
+    if (dot(n, n) == 0.0f) return false;
+    const F4 w0 = sub(pos, V0);
+    const F4 disp = mul(vel, P.deltaTime);
+    const float a = dot(n, w0);
+    if (a < 0.0f) return false;
+    const float b = dot(n, disp);
+    if (std::fabs(b) < 0.000001f) return false;
+    const float r = -a / b;
+    if (r < 0.0f) return false;
+    const F4 I = add(pos, mul(disp, r));
+    const float uu = dot(u, u), uv = dot(u, v), vv = dot(v, v);
+    const F4 w = sub(I, V0);
+    const float wu = dot(w, u), wv = dot(w, v);
+    const float D = uv * uv - uu * vv;
+    const float s = (uv * wv - vv * wu) / D;
+    if (s < 0.0f || s > 1.0f) return false;
+    const float t = (uv * wu - uu * wv) / D;
+    if (t < 0.0f || (s + t) > 1.0f) return false;
+    n = normalize(n);
+    const F4 Vc = sub(add(pos, disp), V0);
+    const float dist = dot(Vc, n);
+    const float depth = P.particleRadius - dist;
+    if (depth > 0.0f) {
+        const F4 dPos = mul(mul(normalize(disp), dot(n, disp)), depth);
+        const F4 dTan = sub(vel, mul(n, dot(n, vel)));
+        force = add(force, divs(dTan, P.deltaTime));
+        const float hd = P.cellSize - dist;
+        force = add(force, mul(mul(mul(mul(n, hd), hd), P.pressureConstant / P.density), P.mass));
+        pos = add(pos, dPos);
+        vel = {0.0f, 0.0f, 0.0f, 0.0f};
+        return true;
+    }
+    return false;
+}
+
+bool collide_box(const gbsph_bvh_node& nd, F4 pos, F4 vel, float radius) {
+    const F4 nr = normalize(vel);
+    const F4 inv = {1.0f / nr.x, 1.0f / nr.y, 1.0f / nr.z, 1.0f / nr.w};
+    const F4 bmin = {nd.bbMin[0], nd.bbMin[1], nd.bbMin[2], nd.bbMin[3]};
+    const F4 bmax = {nd.bbMax[0], nd.bbMax[1], nd.bbMax[2], nd.bbMax[3]};
+    const F4 tbot = mulv(inv, sub(bmin, pos)), ttop = mulv(inv, sub(bmax, pos));
+    const float tminx = clmin(ttop.x, tbot.x), tminy = clmin(ttop.y, tbot.y), tminz = clmin(ttop.z, tbot.z);
+    const float tmaxx = clmax(ttop.x, tbot.x), tmaxy = clmax(ttop.y, tbot.y), tmaxz = clmax(ttop.z, tbot.z);
+    const float tnear = clmax(clmax(tminx, tminy), clmax(tminx, tminz));
+    const float tfar = clmin(clmin(tmaxx, tmaxy), clmin(tmaxx, tmaxz));
+    if (!(tfar > tnear)) return false;
+    return tnear < clmax(radius, len(vel));
+}
+
+}  // namespace
+
+extern "C" {
+
+// position / velocity / force: float4[np], updated in place for the particles that collide.
+void orc_bvh_collide(const gbsph_fluid3d_params* P, float* position, float* velocity, float* force, uint32_t np,
+                     const gbsph_bvh_node* bvh, uint32_t root, const uint32_t* index, const float* vertex) {
+    for (uint32_t p = 0; p < np; p++) {
+        F4 pos = load(position, p), vel = load(velocity, p), frc = load(force, p);
+        uint32_t queue[256];
+        uint32_t head = 0, tail = 1;
+        queue[0] = root;
+        while (head != tail) {
+            const uint32_t it = queue[head];
+            head = (head + 1) % 256;
+            const uint32_t l = (uint32_t)bvh[it].left, r = (uint32_t)bvh[it].right;
+            if (l == r) {
+                if (collide_triangle(bvh[it].bit * 3, index, vertex, pos, vel, frc, *P)) {
+                    store(position, p, pos);
+                    store(velocity, p, vel);
+                    store(force, p, frc);
+                    break;
+                }
+            } else {
+                if (collide_box(bvh[l], pos, vel, P->particleRadius)) {
+                    queue[tail] = l;
+                    tail = (tail + 1) % 256;
+                }
+                if (collide_box(bvh[r], pos, vel, P->particleRadius)) {
+                    queue[tail] = r;
+                    tail = (tail + 1) % 256;
+                }
+            }
+        }
+    }
 }
 
 }  // extern "C"

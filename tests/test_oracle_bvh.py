@@ -53,3 +53,31 @@ def test_bvh_oracle_box_only_grows():
     v2[:, :3] *= 0.25
     oracle.bvh_build(v2, idx, box)
     np.testing.assert_array_equal(box, first)  # a smaller mesh does not shrink it
+
+
+def test_bvh_oracle_collide_stops_particles_crossing_the_mesh():
+    """Particles just outside a sphere mesh moving inward: those whose step crosses a
+    triangle within the particle radius stop (velocity 0) and are pushed; the others are left
+    as they were."""
+    from libcl_gb300 import default_params
+    from libcl_gb300.scenes import SplitMix64
+    v, idx = sphere_mesh(16, 32)
+    box = np.zeros(8, np.float32)
+    nodes, root, _, _ = oracle.bvh_build(v, idx, box)
+    p = default_params()
+    rng = SplitMix64(5)
+    n = 2000
+    d = rng.normal(3 * n).reshape(n, 3)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    pos[:, :3] = 1.0 + d * (0.505 + 0.002 * rng.uniform(n))[:, None]
+    vel[:, :3] = -d * 2.0
+    force = np.zeros_like(pos)
+    p0, v0 = pos.copy(), vel.copy()
+    oracle.bvh_collide(p, pos, vel, force, nodes, root, idx, v)
+    hit = np.all(vel == 0, axis=1)
+    assert hit.sum() > n // 2
+    np.testing.assert_array_equal(pos[~hit], p0[~hit])
+    np.testing.assert_array_equal(vel[~hit], v0[~hit])
+    assert np.all(np.any(pos[hit] != p0[hit], axis=1))
