@@ -232,6 +232,10 @@ GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream);
 GBSPH_API int gbsph_fluid3d_get_cell_bounds(gbsph_fluid3d_t h, uint32_t* cell_start,
                                             uint32_t* cell_end, size_t n_cells, void* stream);
 GBSPH_API int gbsph_fluid3d_sync_status(gbsph_fluid3d_t h, void* stream);
+/* clEmitter (libCL/phys/oclFluid3D.cl:273-282; the reference's compute() does not enqueue
+ * it): particles emit+1 .. emit+99 of the position/velocity buffers are placed on a sheet at
+ * y = 0.6 (10 per row, 2 particleRadius apart) with velocity (0, emit_speed, 0). */
+GBSPH_API int gbsph_fluid3d_emit(gbsph_fluid3d_t h, uint32_t emit, float emit_speed, void* stream);
 /* With GBSPH_OPT_PROFILE on: waits for the last profiled compute() and writes the duration
  * in milliseconds of each of its stages (front end = scratch clear + hash, sort passes incl.
  * the fused reorder, cell bounds, density, forces + integration) into ms[0..4]. Returns the
@@ -357,6 +361,9 @@ GBSPH_API int gbsph_fluid2d_compute_border(gbsph_fluid2d_t h, const float* mask,
                                            void* stream);
 /* compute(oclDevice&) -- libCL/phys/oclFluid2D.cpp:256-362. */
 GBSPH_API int gbsph_fluid2d_compute(gbsph_fluid2d_t h, void* stream);
+/* clEmitter (libCL/phys/oclFluid2D.cl:342-352; the reference's compute() does not enqueue
+ * it): particle emit + 1 is placed at x = 1 with velocity (25, 1). */
+GBSPH_API int gbsph_fluid2d_emit(gbsph_fluid2d_t h, uint32_t emit, void* stream);
 /* The cell table as two uint32 arrays of n_cells (= the compiled table size) entries. */
 GBSPH_API int gbsph_fluid2d_get_cell_bounds(gbsph_fluid2d_t h, uint32_t* cell_start, uint32_t* cell_end,
                                             size_t n_cells, void* stream);

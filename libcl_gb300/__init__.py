@@ -128,6 +128,8 @@ SIGNATURES = {
     "gbsph_fluid2d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
     "gbsph_fluid2d_sync_status": (_I, [_P, _P]),
     "gbsph_fluid2d_last_error": (C.c_char_p, [_P]),
+    "gbsph_fluid2d_emit": (_I, [_P, C.c_uint32, _P]),
+    "gbsph_fluid3d_emit": (_I, [_P, C.c_uint32, C.c_float, _P]),
     "gbsph_bvh_create": (_I, [C.POINTER(_P)]),
     "gbsph_bvh_destroy": (_I, [_P]),
     "gbsph_bvh_compute": (_I, [_P, _P, _SZ, _P, _SZ, _P]),
@@ -363,6 +365,10 @@ class Fluid3D:
 
     def sync_status(self, stream=None) -> int:
         return self._lib.gbsph_fluid3d_sync_status(self._h, _stream(stream))
+
+    def emit(self, emit: int, emit_speed: float, stream=None) -> None:
+        """clEmitter: particles emit+1 .. emit+99 start on a sheet at y = 0.6."""
+        self._check(self._lib.gbsph_fluid3d_emit(self._h, emit, emit_speed, _stream(stream)))
 
     def stage_times(self) -> dict:
         """Per-stage milliseconds of the last compute() run with OPT_PROFILE on."""
@@ -614,6 +620,10 @@ class Fluid2D:
 
     def sync_status(self, stream=None) -> int:
         return self._lib.gbsph_fluid2d_sync_status(self._h, _stream(stream))
+
+    def emit(self, emit: int, stream=None) -> None:
+        """clEmitter: particle emit+1 enters at x = 1 with velocity (25, 1)."""
+        self._check(self._lib.gbsph_fluid2d_emit(self._h, emit, _stream(stream)))
 
 
 def default_params_2d() -> Fluid2DParams:

@@ -281,6 +281,22 @@ __global__ void k2_border(const float4* __restrict__ mask, int w, int h, float4*
 
 int grid1(uint32_t n) { return (int)((n + 255) / 256); }
 
+// clEmitter (libCL/phys/oclFluid2D.cl:342-352): particle emit+1 enters at x = 1 on one of
+// four heights, with velocity (25, 1); the sixth field (`age` there) is set to 1.
+__global__ void k2_emitter(P2* __restrict__ state, uint32_t n, uint32_t emit, float psize) {
+    const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
+    if (particle >= n) return;
+    if (particle > emit && particle < emit + 2u) {
+        P2 q = state[particle];
+        q.px = 1.0f;
+        q.py = __fadd_rn(14.0f, __fmul_rn((float)(particle % 4u * 12u), psize));
+        q.vx = 25.0f;
+        q.vy = 1.0f;
+        q.unused = 1.0f;
+        state[particle] = q;
+    }
+}
+
 }  // namespace
 
 struct gbsph_fluid2d_s {
@@ -603,6 +619,16 @@ GBSPH_API int gbsph_fluid2d_compute_border(gbsph_fluid2d_t h, const float* mask,
     const float s = (float)((double)(dX * dY) / (2 * M_PI * (double)p.particleSize * (double)p.particleSize));
     const dim3 blk(16, 16), grd((width + 15) / 16, (height + 15) / 16);
     k2_border<<<grd, blk, 0, (cudaStream_t)stream>>>((const float4*)mask, width, height, h->bvec, h->bstate, k, s);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_fluid2d_emit(gbsph_fluid2d_t h, uint32_t emit, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "emit before compile()");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    k2_emitter<<<(unsigned)((h->n + 255) / 256), 256, 0, (cudaStream_t)stream>>>((P2*)h->state, (uint32_t)h->n, emit,
+                                                                                h->params.particleSize);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }

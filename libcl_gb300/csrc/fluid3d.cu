@@ -749,6 +749,16 @@ GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream) {
     }
 }
 
+GBSPH_API int gbsph_fluid3d_emit(gbsph_fluid3d_t h, uint32_t emit, float emit_speed, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "emit before compile()");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    k_emitter<<<grid1((uint32_t)h->n), 256, 0, (cudaStream_t)stream>>>(P4(h, 0), P4(h, 1), (uint32_t)h->n, emit,
+                                                                        emit_speed, h->params.particleRadius);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    return GBSPH_OK;
+}
+
 GBSPH_API int gbsph_fluid3d_get_cell_bounds(gbsph_fluid3d_t h, uint32_t* cell_start, uint32_t* cell_end,
                                             size_t n_cells, void* stream) {
     if (!h) return GBSPH_ERR_ARGUMENT;

@@ -62,3 +62,21 @@ def test_fluid2d_borrowed_state_and_reference_default_count(cuda):
     torch.cuda.synchronize()
     assert torch.isfinite(st).all()
     assert f.getStateBuffer().data_ptr() == st.data_ptr()
+
+
+def test_fluid2d_emitter(cuda):
+    """clEmitter (libCL/phys/oclFluid2D.cl:342-352): only particle emit+1 changes."""
+    import torch
+    f = Fluid2D()
+    f.compile()
+    st = block_state(64, 64)
+    f.setParticleCount(st.shape[0])
+    f.getStateBuffer().copy_(torch.from_numpy(st))
+    f.emit(101)
+    torch.cuda.synchronize()
+    g = f.getStateBuffer().cpu().numpy()
+    want = st.copy()
+    psize = np.float32(f.getParameters().particleSize)
+    want[102, :4] = [1.0, np.float32(14.0) + np.float32(102 % 4 * 12) * psize, 25.0, 1.0]
+    want[102, 5] = 1.0
+    np.testing.assert_array_equal(g.view(np.uint32), want.view(np.uint32))

@@ -371,3 +371,23 @@ def test_dam_break_2d_fused_steps_fed_identical_state(cuda):
         r = oracle.step(pos, v, frc, sc.params)
         compare_fast(g, gs, r, {"pos": pos, "vel": v, "force": frc}, before["pos"])
     assert f.sync_status() == OK
+
+
+def test_emitter(cuda):
+    """clEmitter (libCL/phys/oclFluid3D.cl:273-282): particles emit+1 .. emit+99 move to the
+    sheet, the rest keep their state; C's truncating integer division and remainder of the
+    negative index."""
+    sc = block_collapse_3d(8, 8, 8)
+    vel = perturbed(sc)
+    f = make_fluid(sc, vel=vel)
+    f.emit(200, 1.5)
+    g = state(f)
+    r = np.float32(sc.params.particleRadius)
+    pos, v = sc.pos.copy(), vel.copy()
+    for p in range(201, 300):
+        index = 200 - p
+        q, m = int(index / 10), int(np.fmod(index, 10))
+        pos[p] = [np.float32(q * 2) * r, 0.6, np.float32(0.6) + np.float32(m * 2) * r, 1.0]
+        v[p] = [0.0, 1.5, 0.0, 1.0]
+    np.testing.assert_array_equal(g["pos"].view(np.uint32), pos.astype(np.float32).view(np.uint32))
+    np.testing.assert_array_equal(g["vel"], v)
