@@ -80,17 +80,21 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
         if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
 }
 
+// Resident CTAs per SM the register budget is set for: shared memory caps a 4096-key tile at
+// five (42 KB each), a 2048-key tile fits six at 40 registers without spills.
+constexpr int onesweep_min_blocks(int items) { return items == 16 ? 5 : 6; }
+
 template <bool IOTA, int NGATHER, int ITEMS>
-__global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
+__global__ void __launch_bounds__(SORT_THREADS, onesweep_min_blocks(ITEMS)) k_onesweep(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
     int bits, int pass, uint32_t tiles, uint32_t* __restrict__ scratch, uint32_t* err,
     SortGather gather) {
+    static_assert(ITEMS % 2 == 0, "ranks are packed two per register");
     constexpr int TILE = SORT_THREADS * ITEMS;
     __shared__ uint32_t s_keys[TILE];
     __shared__ uint32_t s_vals[TILE];
     __shared__ uint32_t s_whist[SORT_WARPS * SORT_RADIX];
-    __shared__ uint32_t s_tile_start[SORT_RADIX];
     __shared__ uint32_t s_base[SORT_RADIX];
     __shared__ uint32_t s_tmp[SORT_WARPS];
     __shared__ uint32_t s_tile;
@@ -112,41 +116,43 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
     const uint32_t mask = (1u << bits) - 1u;
 
     // Load: warp-striped, so item order inside the tile is (warp, i, lane) == index order.
-    uint32_t k[ITEMS], v[ITEMS], r[ITEMS];
+    // The keys wait in the value half of the tile buffer (each warp its own slice) until the
+    // scatter, which keeps the register count low enough for five CTAs per SM.
+    uint32_t* stash = s_vals + warp * 32 * ITEMS + lane;
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
         const uint32_t idx = base + (uint32_t)(warp * 32 * ITEMS + i * 32 + lane);
-        const bool in = idx < n;
-        k[i] = in ? keys_in[idx] : 0xFFFFFFFFu;  // padding sorts last in the top digit
-        v[i] = IOTA ? idx : (in ? vals_in[idx] : 0u);
+        stash[i * 32] = idx < n ? keys_in[idx] : 0xFFFFFFFFu;  // padding sorts last in the top digit
     }
+    __syncwarp();
 
-    // Rank within the warp: peers of equal digit via ballots; the lowest peer lane updates
-    // the warp's private digit counter and broadcasts the old value.
+    // Rank within the warp: peers of equal digit = AND over the digit's bits of the ballot or
+    // its complement (digits narrower than 8 bits have zero high bits, whose ballots are
+    // empty and leave the mask alone). All peers read the warp's digit counter, then the
+    // lowest peer advances it. Ranks are < 2^16 and stored two per register.
     uint32_t* wh = s_whist + warp * SORT_RADIX;
     const uint32_t lt = lanemask_lt();
+    uint32_t r[ITEMS / 2];
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = (k[i] >> shift) & mask;
+        const uint32_t d = (stash[i * 32] >> shift) & mask;
         uint32_t peers = 0xffffffffu;
-        for (int b = 0; b < bits; ++b) {
+#pragma unroll
+        for (int b = 0; b < SORT_RADIX_BITS; ++b) {
             const uint32_t bit = (d >> b) & 1u;
-            const uint32_t m = __ballot_sync(0xffffffffu, bit);
-            peers &= bit ? m : ~m;
+            peers &= __ballot_sync(0xffffffffu, bit) ^ (bit - 1u);
         }
-        const uint32_t leader = __ffs(peers) - 1;
-        uint32_t old = 0;
-        if ((uint32_t)lane == leader) {
-            old = wh[d];
-            wh[d] = old + __popc(peers);
-        }
-        old = __shfl_sync(0xffffffffu, old, leader);
-        r[i] = old + __popc(peers & lt);
+        const uint32_t old = wh[d];
+        __syncwarp();
+        if ((uint32_t)lane == __ffs(peers) - 1u) wh[d] = old + __popc(peers);
+        const uint32_t rank = old + __popc(peers & lt);
+        r[i >> 1] = (i & 1) ? (r[i >> 1] | rank << 16) : rank;
         __syncwarp();
     }
     __syncthreads();
 
-    // Thread t owns digit t: warp-exclusive offsets, tile count, tile-local start.
+    // Thread t owns digit t: tile count, then each warp's start of digit t inside the tile
+    // (tile-local start + the counts of the warps before it).
     uint32_t cnt = 0;
 #pragma unroll
     for (int w = 0; w < SORT_WARPS; ++w) {
@@ -155,7 +161,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         cnt += c;
     }
     const uint32_t tstart = block_exclusive_scan(cnt, s_tmp);
-    s_tile_start[t] = tstart;
+#pragma unroll
+    for (int w = 0; w < SORT_WARPS; ++w) s_whist[w * SORT_RADIX + t] += tstart;
     const uint32_t goff = block_exclusive_scan(hist[t], s_tmp);
 
     // Decoupled look-back for digit t.
@@ -182,15 +189,18 @@ __global__ void __launch_bounds__(SORT_THREADS) k_onesweep(
         st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_PREFIX | ((excl + cnt) & COUNT_MASK));
     }
     s_base[t] = goff + excl - tstart;
+    uint32_t k[ITEMS];
+#pragma unroll
+    for (int i = 0; i < ITEMS; ++i) k[i] = stash[i * 32];
     __syncthreads();
 
-    // Tile-local sorted order in shared memory.
+    // Tile-local sorted order in shared memory; values are read here, after the ranking.
 #pragma unroll
     for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = (k[i] >> shift) & mask;
-        const uint32_t pos = s_tile_start[d] + s_whist[warp * SORT_RADIX + d] + r[i];
+        const uint32_t idx = base + (uint32_t)(warp * 32 * ITEMS + i * 32 + lane);
+        const uint32_t pos = s_whist[warp * SORT_RADIX + ((k[i] >> shift) & mask)] + ((r[i >> 1] >> (16 * (i & 1))) & 0xffffu);
         s_keys[pos] = k[i];
-        s_vals[pos] = v[i];
+        s_vals[pos] = IOTA ? idx : (idx < n ? vals_in[idx] : 0u);
     }
     __syncthreads();
 
