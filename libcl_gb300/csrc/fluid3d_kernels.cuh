@@ -958,13 +958,13 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
             }
             __syncthreads();
         }
-        // P = 4 lanes per target: the brick's targets are consecutive in the centre row, so the
-        // CTA takes 64 of them at a time whatever cell they are in; lane p of a target takes
-        // every 4th entry of its list (or, scanning, every 4th candidate of each row) and the 4
-        // partial sums are added with shuffles. The summation order depends on neither the
+        // P = 2 lanes per target: the brick's targets are consecutive in the centre row, so the
+        // CTA takes 128 of them at a time whatever cell they are in; the two lanes of a target
+        // split its list (or, scanning, take alternate candidates of each row) and their
+        // partial sums are added with a shuffle. The summation order depends on neither the
         // brick width nor the brick's target count.
         const uint32_t tbeg = S.off[RC][1];
-        constexpr uint32_t lp = 2u, P = 1u << lp;
+        constexpr uint32_t lp = 1u, P = 1u << lp;
         for (uint32_t u0 = 0; u0 < ntarg; u0 += BRICK_THREADS >> lp) {
             const uint32_t u = u0 + ((uint32_t)t >> lp), p = (uint32_t)t & (P - 1u);
             const bool active = u < ntarg;
@@ -995,30 +995,35 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                 const uint64_t meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
                 const bool scan = (meta & NBR_SCAN) != 0;
                 if (!scan) {
-                    // With four sub-lists lane p takes sub-list p; otherwise the Q sub-lists
-                    // are one sequence and lane p takes its entries p, p + 4, ..., two at a time
-                    // so that their loads overlap (slot s of the target's list sits at
-                    // chunk-major position ((s >> 3) * ntarg + u) * 8 + (s & 7))
+                    // When the sub-lists start on 16-byte chunks and pair up (Q = 2, 4, 8),
+                    // lane p walks sub-lists p, p + 2, ... chunk by chunk; otherwise the Q
+                    // sub-lists are one sequence and lane p takes its entries p, p + 2, ...,
+                    // two at a time so that their loads overlap (slot s of the target's list
+                    // sits at chunk-major position ((s >> 3) * ntarg + u) * 8 + (s & 7))
                     const uint16_t* lst = (lists_staged ? s_lists : nbr + (size_t)tfirst * NBR_CAP) + (gi - tfirst) * 8u;
                     const uint32_t n8 = ntarg * 8u;
                     uint32_t before = 0;  // entries of the earlier sub-lists
-                    if (Q == P) {  // one sub-list per lane (16 slots, two 16-byte chunks)
-                        const uint32_t n = (uint32_t)(meta >> (8 * p)) & 127u;
-                        const uint4* l4 = reinterpret_cast<const uint4*>(lst);
-                        for (uint32_t k0 = 0; k0 < n; k0 += 8) {
-                            const uint4 v = l4[(size_t)((p * sub + k0) >> 3) * ntarg];
-                            const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-                            const uint32_t m = min(8u, n - k0);
+                    const bool whole = (Q % P) == 0 && (sub & 7u) == 0;
+                    if (whole) {
+#pragma unroll 1
+                        for (uint32_t q = p; q < Q; q += P) {
+                            const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u;
+                            const uint4* l4 = reinterpret_cast<const uint4*>(lst);
+                            for (uint32_t k0 = 0; k0 < n; k0 += 8) {
+                                const uint4 v = l4[(size_t)((q * sub + k0) >> 3) * ntarg];
+                                const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+                                const uint32_t m = min(8u, n - k0);
 #pragma unroll
-                            for (uint32_t e = 0; e < 8; ++e) {
-                                if (e >= m) break;
-                                const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
-                                force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
+                                for (uint32_t e = 0; e < 8; ++e) {
+                                    if (e >= m) break;
+                                    const uint32_t idx = (w[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                                    force_pair_pre<DIMS>(pi, vi, s_pos[idx], s_vel[idx], kp.h, acc);
+                                }
                             }
                         }
                     }
 #pragma unroll 1
-                    for (uint32_t q = 0; q < (Q == P ? 0u : Q); ++q) {
+                    for (uint32_t q = 0; q < (whole ? 0u : Q); ++q) {
                         const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u, b = q * sub;
                         uint32_t k = (p - before) & (P - 1u);
                         for (; k + P < n; k += 2 * P) {
