@@ -52,6 +52,18 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
+// Shared-memory load / store by 32-bit shared-window address (volatile: they stay in program
+// order with each other and with the barriers around them; the store also orders the
+// compiler's own shared-memory accesses around it).
+__device__ __forceinline__ float4 lds_f4(uint32_t a) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
+__device__ __forceinline__ void sts_u16(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.u16 [%0], %1;" ::"r"(a), "h"((uint16_t)v) : "memory");
+}
+
 // ---- mbarrier + cp.async.bulk (global -> shared, no tensor map) ----------------------
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {

@@ -721,6 +721,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
     uint32_t phase = 0;
     const uint32_t n_bricks = counters[0];
     const float h2 = kp.h2, thr = kp.r2_thresh;
+    const uint32_t buf_a = smem_addr(s_buf);
     // the next brick's id is fetched while this one is processed
     if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
     for (;;) {
@@ -746,15 +747,19 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                 uint16_t* my = wlist + ti * WLIST_STRIDE + q * sub;
                 float acc = 0.0f;
                 uint32_t nk = 0;  // in-range candidates of this lane (the target itself included)
-                if (active) {
+                if (active && staged) {
+                    // 32-bit shared-memory addresses stepped per candidate: the candidate's
+                    // position (16 bytes) and this lane's next list slot.
+                    const uint32_t my_a = smem_addr(my), last = sub - 1u, step = Q * 16u;
 #pragma unroll 1
                     for (int r = 0; r < R; ++r) {
                         const uint32_t lo = S.off[r][c], len = S.off[r][c + 3] - lo;
-                        const float4* rp = staged ? s_buf + S.base[r] + lo : spos + S.lo[r] + lo;
-                        const uint32_t s0 = S.base[r] + lo;
+                        uint32_t v = S.base[r] + lo + q;  // staged index of the candidate
+                        uint32_t a = buf_a + v * 16u;
+                        const uint32_t a_end = buf_a + (S.base[r] + lo + len) * 16u;
 #pragma unroll 4
-                        for (uint32_t k = q; k < len; k += Q) {
-                            const float4 pj = rp[k];
+                        for (; a < a_end; a += step, v += Q) {
+                            const float4 pj = lds_f4(a);
                             const float dx = pi.x - pj.x, dy = pi.y - pj.y;
                             float r2 = fmaf(dy, dy, dx * dx);
                             if (DIMS == 3) {
@@ -769,7 +774,26 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                             // Once the sub-list is full, later candidates overwrite its last
                             // entry, so a full sub-list counts as an overflow. The target and
                             // coincident particles (r^2 = 0) are listed; the force pass skips them.
-                            my[min(nk, sub - 1)] = (uint16_t)(s0 + k);
+                            sts_u16(my_a + 2u * min(nk, last), v);
+                            nk += in ? 1u : 0u;
+                        }
+                    }
+                } else if (active) {  // unstaged brick: candidates from global memory, no lists
+#pragma unroll 1
+                    for (int r = 0; r < R; ++r) {
+                        const uint32_t lo = S.off[r][c], len = S.off[r][c + 3] - lo;
+                        const float4* rp = spos + S.lo[r] + lo;
+                        for (uint32_t k = q; k < len; k += Q) {
+                            const float4 pj = rp[k];
+                            const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+                            float r2 = fmaf(dy, dy, dx * dx);
+                            if (DIMS == 3) {
+                                const float dz = pi.z - pj.z;
+                                r2 = fmaf(dz, dz, r2);
+                            }
+                            const bool in = r2 < thr;
+                            const float tt = in ? h2 - r2 : 0.0f;
+                            acc = fmaf(tt * tt, tt, acc);
                             nk += in ? 1u : 0u;
                         }
                     }
