@@ -362,6 +362,31 @@ def extra_bvh(stream) -> dict:
             "cpu_reference_port_ms": cpu_s * 1e3, "cpu_cores": 1}
 
 
+def extra_bvh_lines(stream) -> dict:
+    """The 2D segment BVH build (oclBvhLines): 1,000,000 short segments on a 1000^2 lattice
+    of distinct integer midpoints, shuffled; one build = Morton keys, 32-bit sort, nodes,
+    links, leaves, boxes. The CPU restatement of the reference build, single-threaded, on the
+    same segments beside it."""
+    import torch
+    import oracle
+    from libcl_gb300 import BvhLines
+    from libcl_gb300.scenes import segment_lattice
+    v = segment_lattice(1000)
+    dv = torch.from_numpy(v).cuda()
+    b = BvhLines()
+    for _ in range(3):
+        b.compute(dv, stream)
+    ts = [_time_steps(lambda: b.compute(dv, stream), 1, stream) for _ in range(10)]
+    assert b.sync_status() == 0
+    ms = statistics.median(ts)
+    t0 = time.perf_counter()
+    oracle.bvh_lines_build(v)
+    cpu_s = time.perf_counter() - t0
+    n = v.shape[0] // 2
+    return {"segments": n, "ms": ms, "segments_per_s": n / (ms * 1e-3),
+            "cpu_reference_port_ms": cpu_s * 1e3, "cpu_cores": 1}
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU port of the reference kernels on a bounded sample."""
     if rank != 0:
@@ -536,7 +561,8 @@ def main(argv=None) -> int:
             torch.cuda.empty_cache()
             result["extras"] = {"batched_256_scenes": extra_batched(stream), "sort_16m": extra_sort(stream),
                                 "two_d": extra_2d(stream), "adjoint": extra_adjoint(stream),
-                                "bvh_1m_triangles": extra_bvh(stream)}
+                                "bvh_1m_triangles": extra_bvh(stream),
+                                "bvh_lines_1m_segments": extra_bvh_lines(stream)}
         if world == 1 and not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
     if rank == 0:

@@ -428,6 +428,45 @@ GBSPH_API int gbsph_bvh_collide(gbsph_bvh_t h, const gbsph_fluid3d_params* param
                                 size_t n_vertices, const uint32_t* index, void* stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Linear BVH over 2D line segments. Replaces `oclBvhLines` (libCL/geom/oclBvhLines.h:20-77,
+ * libCL/geom/oclBvhLines.cpp:18-132), the 2D sibling of oclBvhTrimesh: Morton key of each
+ * segment's midpoint taken directly as 16-bit integer coordinates (no global box) -> 32-bit
+ * sort -> internal nodes split at the highest differing key bit (31..0), linked to the nearer
+ * higher-bit neighbour -> leaves -> boxes. The node layout is the reference's 32-byte BVHNode
+ * (libCL/geom/oclBvhLines.h:28-36): nodes [0, n-1) internal, nodes [n-1, 2n-1) leaves
+ * (left == right == 0, bit = segment index); internal nodes end with trav = 3 (the reference's
+ * second visitor swaps the first visitor's 2 for 3). Midpoint coordinates are converted to
+ * integers by truncation; the reference leaves negative coordinates and coordinates of 2^32
+ * or more undefined, here they become 0 and 0xFFFFFFFF. Repeated keys: as gbsph_bvh.
+ * ---------------------------------------------------------------------------------------- */
+typedef struct gbsph_bvh2d_node {
+    float bbMin[2];
+    float bbMax[2];
+    int32_t left;
+    int32_t right;
+    uint32_t bit;
+    uint32_t trav;
+} gbsph_bvh2d_node;
+
+typedef struct gbsph_bvh_lines_s* gbsph_bvh_lines_t;
+
+/* oclBvhLines(oclContext&, oclProgram* parent) -- libCL/geom/oclBvhLines.cpp:18-42. */
+GBSPH_API int gbsph_bvh_lines_create(gbsph_bvh_lines_t* out);
+GBSPH_API int gbsph_bvh_lines_destroy(gbsph_bvh_lines_t h);
+/* compute(oclDevice&, oclBuffer& vertex) -- libCL/geom/oclBvhLines.cpp:48-115: `vertex` is a
+ * device float2[n_vertices], two per segment (n_vertices / 2 >= 2 segments; an odd last
+ * vertex is ignored, as the reference's integer division does). Asynchronous on `stream`. */
+GBSPH_API int gbsph_bvh_lines_compute(gbsph_bvh_lines_t h, const float* vertex, size_t n_vertices, void* stream);
+/* getNodeBuffer / getNodeCount -- libCL/geom/oclBvhLines.cpp:123-131. */
+GBSPH_API gbsph_bvh2d_node* gbsph_bvh_lines_get_node_buffer(gbsph_bvh_lines_t h, size_t* count);
+GBSPH_API size_t gbsph_bvh_lines_get_node_count(gbsph_bvh_lines_t h);
+/* getRootNode -- libCL/geom/oclBvhLines.cpp:118-121: synchronises `stream`. */
+GBSPH_API int gbsph_bvh_lines_get_root_node(gbsph_bvh_lines_t h, uint32_t* root, void* stream);
+/* Synchronises `stream` and reports (and clears) device-side errors. */
+GBSPH_API int gbsph_bvh_lines_sync_status(gbsph_bvh_lines_t h, void* stream);
+GBSPH_API const char* gbsph_bvh_lines_last_error(gbsph_bvh_lines_t h);
+
+/* ------------------------------------------------------------------------------------------
  * Adjoint of the 3D step (no counterpart in the reference, which has no derivatives):
  * reverse-mode gradients of a loss on the state after `steps` gbsph_fluid3d_compute() calls
  * with respect to the initial positions and velocities, the gas constant (stiffness) and the

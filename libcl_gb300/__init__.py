@@ -140,6 +140,14 @@ SIGNATURES = {
     "gbsph_bvh_sync_status": (_I, [_P, _P]),
     "gbsph_bvh_last_error": (C.c_char_p, [_P]),
     "gbsph_bvh_collide": (_I, [_P, C.POINTER(Fluid3DParams), _P, _P, _P, _SZ, _P, _SZ, _P, _P]),
+    "gbsph_bvh_lines_create": (_I, [C.POINTER(_P)]),
+    "gbsph_bvh_lines_destroy": (_I, [_P]),
+    "gbsph_bvh_lines_compute": (_I, [_P, _P, _SZ, _P]),
+    "gbsph_bvh_lines_get_node_buffer": (_P, [_P, C.POINTER(_SZ)]),
+    "gbsph_bvh_lines_get_node_count": (_SZ, [_P]),
+    "gbsph_bvh_lines_get_root_node": (_I, [_P, C.POINTER(C.c_uint32), _P]),
+    "gbsph_bvh_lines_sync_status": (_I, [_P, _P]),
+    "gbsph_bvh_lines_last_error": (C.c_char_p, [_P]),
     "gbsph_adjoint3d_create": (_I, [C.POINTER(_P), _P, C.c_uint32, C.c_uint32]),
     "gbsph_adjoint3d_destroy": (_I, [_P]),
     "gbsph_adjoint3d_forward": (_I, [_P, _P]),
@@ -488,6 +496,56 @@ class BvhTrimesh:
         self._check(self._lib.gbsph_bvh_collide(self._h, C.byref(params), _ptr(position), _ptr(velocity), _ptr(force),
                                                 position.numel() // 4, _ptr(vertex), vertex.numel() // 4, _ptr(index),
                                                 _stream(stream)))
+
+
+class BvhLines:
+    """oclBvhLines (libCL/geom/oclBvhLines.h:20-77): compute(vertex) builds the BVH of 2D line
+    segments (two float2 vertices each); getNodeBuffer / getNodeCount / getRootNode read it.
+    Nodes are 32-byte records (bbMin[2], bbMax[2], left, right, bit, trav) returned as an int32
+    tensor view [count, 8] (use .view(torch.float32) for the boxes)."""
+
+    NODE_WORDS = 8
+
+    def __init__(self):
+        self._lib = load_library()
+        h = C.c_void_p()
+        rc = self._lib.gbsph_bvh_lines_create(C.byref(h))
+        if rc:
+            raise GbsphError(rc, "gbsph_bvh_lines_create")
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.gbsph_bvh_lines_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise GbsphError(rc, self._lib.gbsph_bvh_lines_last_error(self._h).decode())
+
+    def compute_raw(self, vertex, stream=None) -> int:
+        return self._lib.gbsph_bvh_lines_compute(self._h, _ptr(vertex), vertex.numel() // 2, _stream(stream))
+
+    def compute(self, vertex, stream=None) -> None:
+        """vertex: float32 CUDA tensor [V, 2], two vertices per segment."""
+        self._check(self.compute_raw(vertex, stream))
+
+    def getNodeCount(self) -> int:
+        return int(self._lib.gbsph_bvh_lines_get_node_count(self._h))
+
+    def getNodeBuffer(self):
+        import torch
+        count = C.c_size_t()
+        p = self._lib.gbsph_bvh_lines_get_node_buffer(self._h, C.byref(count))
+        return _device_view(p, count.value * self.NODE_WORDS, torch.int32, (count.value, self.NODE_WORDS))
+
+    def getRootNode(self, stream=None) -> int:
+        r = C.c_uint32()
+        self._check(self._lib.gbsph_bvh_lines_get_root_node(self._h, C.byref(r), _stream(stream)))
+        return r.value
+
+    def sync_status(self, stream=None) -> int:
+        return self._lib.gbsph_bvh_lines_sync_status(self._h, _stream(stream))
 
 
 class Batch3D:

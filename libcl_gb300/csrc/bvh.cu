@@ -1,6 +1,9 @@
 // bvh.cu -- linear BVH over a triangle mesh: the oclBvhTrimesh replacement behind the C ABI
 // (libCL/geom/oclBvhTrimesh.h:20-84, libCL/geom/oclBvhTrimesh.cpp:56-143,
-// libCL/geom/oclBvhTrimesh.cl:33-298). The reference's second user of the radix sort.
+// libCL/geom/oclBvhTrimesh.cl:33-298), the reference's second user of the radix sort; and its
+// 2D sibling over line segments, the oclBvhLines replacement (libCL/geom/oclBvhLines.h:20-77,
+// libCL/geom/oclBvhLines.cpp:48-115, libCL/geom/oclBvhLines.cl:27-245), which shares the node
+// creation, linking, leaves and parent links (templated on the node type).
 //
 // One build, in the reference's order:
 //   global bounding box (accumulated into the handle's box, which starts at zero and is never
@@ -44,6 +47,28 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {  // "code", libCL/geo
     x = (x | (x << 4)) & 0x030C30C3u;
     x = (x | (x << 2)) & 0x09249249u;
     return x;
+}
+
+// 16-bit interleave of clMorton, libCL/geom/oclBvhLines.cl:35-52.
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+    x &= 0x0000FFFFu;
+    x = (x | (x << 8)) & 0x00FF00FFu;
+    x = (x | (x << 4)) & 0x0F0F0F0Fu;
+    x = (x | (x << 2)) & 0x33333333u;
+    x = (x | (x << 1)) & 0x55555555u;
+    return x;
+}
+
+// Empty boxes of clCreateNodes: +-MAXFLOAT in the coordinate lanes (w = 0 for triangles).
+__device__ __forceinline__ void box_init(gbsph_bvh_node& nd) {
+    nd.bbMin[0] = nd.bbMin[1] = nd.bbMin[2] = FLT_MAX;
+    nd.bbMin[3] = 0.f;
+    nd.bbMax[0] = nd.bbMax[1] = nd.bbMax[2] = -FLT_MAX;
+    nd.bbMax[3] = 0.f;
+}
+__device__ __forceinline__ void box_init(gbsph_bvh2d_node& nd) {
+    nd.bbMin[0] = nd.bbMin[1] = FLT_MAX;
+    nd.bbMax[0] = nd.bbMax[1] = -FLT_MAX;
 }
 
 // Per-block min / max of the vertices (all four lanes), combined with the handle's box by the
@@ -114,20 +139,35 @@ __global__ void __launch_bounds__(BVH_THREADS) k_bvh_morton(const uint32_t* __re
     val[g] = g;
 }
 
-// clCreateNodes (libCL/geom/oclBvhTrimesh.cl:119-143) and the block maxima of the bits.
+// clMorton of oclBvhLines (libCL/geom/oclBvhLines.cl:27-55): the segment's midpoint,
+// 0.5 * (v0 + v1), truncated to integers, 16 bits per axis interleaved (x in the even bits).
+__global__ void __launch_bounds__(BVH_THREADS) k_bvh_morton_lines(const float2* __restrict__ vertex, uint32_t n,
+                                                                  uint32_t* __restrict__ key,
+                                                                  uint32_t* __restrict__ val) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const float2 v0 = vertex[2 * g], v1 = vertex[2 * g + 1];
+    const uint32_t cx = __float2uint_rz(__fmul_rn(0.5f, __fadd_rn(v0.x, v1.x)));
+    const uint32_t cy = __float2uint_rz(__fmul_rn(0.5f, __fadd_rn(v0.y, v1.y)));
+    key[g] = spread16(cx) | (spread16(cy) << 1);
+    val[g] = g;
+}
+
+// clCreateNodes (libCL/geom/oclBvhTrimesh.cl:119-143, libCL/geom/oclBvhLines.cl:71-95): the
+// highest bit, of bits [0, TOP], where sorted keys i and i + 1 differ; and the block maxima of
+// the bits.
+template <class Node, int TOP>
 __global__ void __launch_bounds__(BVH_THREADS) k_bvh_nodes(const uint32_t* __restrict__ key, uint32_t m,
-                                                           gbsph_bvh_node* __restrict__ node,
+                                                           Node* __restrict__ node,
                                                            uint8_t* __restrict__ bits, uint8_t* __restrict__ bmax) {
+    constexpr uint32_t MASK = TOP == 31 ? 0xFFFFFFFFu : (1u << (TOP + 1)) - 1u;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t bit = 0;
     if (i < m) {
-        const uint32_t d = (key[i] ^ key[i + 1]) & 0x3FFFFFFFu;
+        const uint32_t d = (key[i] ^ key[i + 1]) & MASK;
         bit = d ? 31u - (uint32_t)__clz(d) : 0u;
-        gbsph_bvh_node nd;
-        nd.bbMin[0] = nd.bbMin[1] = nd.bbMin[2] = FLT_MAX;
-        nd.bbMin[3] = 0.f;
-        nd.bbMax[0] = nd.bbMax[1] = nd.bbMax[2] = -FLT_MAX;
-        nd.bbMax[3] = 0.f;
+        Node nd;
+        box_init(nd);
         nd.left = nd.right = -1;
         nd.bit = bit;
         nd.trav = 0;
@@ -179,13 +219,15 @@ __device__ int nearest_higher(const uint8_t* __restrict__ bits, const uint8_t* _
     return -1;
 }
 
-// clLinkNodes (libCL/geom/oclBvhTrimesh.cl:145-199). Several nodes can only claim the same
-// slot (or the root) when sorted keys repeat (their bits are then 0); the largest claimant
-// wins here, as in a sequential run of the reference's work-items.
+// clLinkNodes (libCL/geom/oclBvhTrimesh.cl:145-199, libCL/geom/oclBvhLines.cl:97-151).
+// Several nodes can only claim the same slot (or the root) when sorted keys repeat (their
+// bits are then 0); the largest claimant wins here, as in a sequential run of the
+// reference's work-items.
+template <class Node>
 __global__ void __launch_bounds__(BVH_THREADS) k_bvh_link(const uint8_t* __restrict__ bits,
                                                           const uint8_t* __restrict__ bmax,
                                                           const uint8_t* __restrict__ smax, int m,
-                                                          gbsph_bvh_node* __restrict__ node,
+                                                          Node* __restrict__ node,
                                                           uint32_t* __restrict__ root) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
@@ -201,18 +243,17 @@ __global__ void __launch_bounds__(BVH_THREADS) k_bvh_link(const uint8_t* __restr
     }
 }
 
-// clCreateLeaves (libCL/geom/oclBvhTrimesh.cl:201-234): leaf n-1+g holds triangle val[g] in
-// .bit and takes the free slot between internal nodes g-1 and g.
+// clCreateLeaves (libCL/geom/oclBvhTrimesh.cl:201-234, libCL/geom/oclBvhLines.cl:153-184):
+// leaf n-1+g holds primitive val[g] in .bit and takes the free slot between internal nodes
+// g-1 and g. (The leaf's box is written by the box pass.)
+template <class Node>
 __global__ void __launch_bounds__(BVH_THREADS) k_bvh_leaves(const uint32_t* __restrict__ val, uint32_t n,
-                                                            gbsph_bvh_node* __restrict__ node) {
+                                                            Node* __restrict__ node) {
     const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
     const uint32_t ls = n - 1, L = ls + g;
-    gbsph_bvh_node nd;
-    nd.bbMin[0] = nd.bbMin[1] = nd.bbMin[2] = FLT_MAX;
-    nd.bbMin[3] = 0.f;
-    nd.bbMax[0] = nd.bbMax[1] = nd.bbMax[2] = -FLT_MAX;
-    nd.bbMax[3] = 0.f;
+    Node nd;
+    box_init(nd);
     nd.left = nd.right = 0;
     nd.bit = val[g];
     nd.trav = 0;
@@ -229,7 +270,8 @@ __global__ void __launch_bounds__(BVH_THREADS) k_bvh_leaves(const uint32_t* __re
 }
 
 // Parent links from the child slots, and the visit counters cleared.
-__global__ void __launch_bounds__(BVH_THREADS) k_bvh_parents(const gbsph_bvh_node* __restrict__ node, uint32_t m,
+template <class Node>
+__global__ void __launch_bounds__(BVH_THREADS) k_bvh_parents(const Node* __restrict__ node, uint32_t m,
                                                              int32_t* __restrict__ parent,
                                                              uint32_t* __restrict__ visits) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -281,6 +323,41 @@ __global__ void __launch_bounds__(BVH_THREADS) k_bvh_refit(const uint32_t* __res
         *reinterpret_cast<float4*>(node[p].bbMin) = a;
         *reinterpret_cast<float4*>(node[p].bbMax) = b;
         node[p].trav = 2;
+        c = p;
+    }
+}
+
+// Boxes of oclBvhLines (clComputeAABBs, libCL/geom/oclBvhLines.cl:186-245): each leaf's box
+// from its segment's two vertices; the second of a node's two children to arrive computes
+// min(left, right) / max(left, right) and goes on up. In the reference the first visitor
+// leaves trav = 2 and the second swaps it for 3 before computing, so internal nodes end with
+// trav = 3.
+__global__ void __launch_bounds__(BVH_THREADS) k_bvh_refit_lines(const float2* __restrict__ vertex, uint32_t n,
+                                                                 gbsph_bvh2d_node* node,
+                                                                 const int32_t* __restrict__ parent,
+                                                                 uint32_t* visits, const uint32_t* __restrict__ root) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const uint32_t L = n - 1 + g;
+    const uint32_t seg = node[L].bit;
+    const float2 v0 = vertex[2 * seg], v1 = vertex[2 * seg + 1];
+    const float2 mn = make_float2(cl_min(cl_min(FLT_MAX, v0.x), v1.x), cl_min(cl_min(FLT_MAX, v0.y), v1.y));
+    const float2 mx = make_float2(cl_max(cl_max(-FLT_MAX, v0.x), v1.x), cl_max(cl_max(-FLT_MAX, v0.y), v1.y));
+    *reinterpret_cast<float4*>(node[L].bbMin) = make_float4(mn.x, mn.y, mx.x, mx.y);
+    const uint32_t rt = *root;
+    int32_t c = (int32_t)L;
+    for (uint32_t depth = 0; depth < 2 * n && (uint32_t)c != rt; ++depth) {
+        const int32_t p = parent[c];
+        if (p < 0) return;  // not reachable from the root (repeated keys)
+        __threadfence();
+        if (atomicAdd(&visits[p], 1u) == 0) return;  // the other child is not done yet
+        __threadfence();
+        const volatile gbsph_bvh2d_node* vn = node;
+        const int32_t l = vn[p].left, r = vn[p].right;
+        const float4 box = make_float4(cl_min(vn[l].bbMin[0], vn[r].bbMin[0]), cl_min(vn[l].bbMin[1], vn[r].bbMin[1]),
+                                       cl_max(vn[l].bbMax[0], vn[r].bbMax[0]), cl_max(vn[l].bbMax[1], vn[r].bbMax[1]));
+        *reinterpret_cast<float4*>(node[p].bbMin) = box;
+        node[p].trav = 3;
         c = p;
     }
 }
@@ -402,13 +479,13 @@ GBSPH_API int gbsph_bvh_compute(gbsph_bvh_t h, const float* vertex, size_t n_ver
     rc = gbsph_radix_sort_compute(h->sort, h->key, h->val, n, n, 0, 32, stream);
     if (rc) return fail(&h->last_error, rc, std::string("sort: ") + gbsph_radix_sort_last_error(h->sort));
     const uint32_t nb = (m + BLK - 1) / BLK;
-    k_bvh_nodes<<<grid(m), BVH_THREADS, 0, s>>>(h->key, m, h->node, h->bits, h->bmax);
+    k_bvh_nodes<gbsph_bvh_node, 29><<<grid(m), BVH_THREADS, 0, s>>>(h->key, m, h->node, h->bits, h->bmax);
     k_bvh_smax<<<(unsigned)((nb + 255) / 256 / (SBLK / BLK) + 1), 256, 0, s>>>(h->bmax, nb, h->smax);
     GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->root, 0, 4, s));
-    k_bvh_link<<<grid(m), BVH_THREADS, 0, s>>>(h->bits, h->bmax, h->smax, (int)m, h->node, h->root);
-    k_bvh_leaves<<<grid(n), BVH_THREADS, 0, s>>>(h->val, n, h->node);
+    k_bvh_link<gbsph_bvh_node><<<grid(m), BVH_THREADS, 0, s>>>(h->bits, h->bmax, h->smax, (int)m, h->node, h->root);
+    k_bvh_leaves<gbsph_bvh_node><<<grid(n), BVH_THREADS, 0, s>>>(h->val, n, h->node);
     GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->parent, 0xFF, (2 * (size_t)n - 1) * 4, s));
-    k_bvh_parents<<<grid(m), BVH_THREADS, 0, s>>>(h->node, m, h->parent, h->visits);
+    k_bvh_parents<gbsph_bvh_node><<<grid(m), BVH_THREADS, 0, s>>>(h->node, m, h->parent, h->visits);
     k_bvh_refit<<<grid(n), BVH_THREADS, 0, s>>>(index, v4, n, nv, h->node, h->parent, h->visits, h->root);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     h->n = n;
@@ -637,3 +714,142 @@ extern "C" GBSPH_API int gbsph_bvh_collide(gbsph_bvh_t h, const gbsph_fluid3d_pa
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// oclBvhLines replacement.
+// ------------------------------------------------------------------------------------------
+struct gbsph_bvh_lines_s {
+    int device = 0;
+    gbsph_radix_sort_t sort = nullptr;
+    uint32_t cap = 0;  // segments the buffers hold
+    uint32_t n = 0;    // segments of the last build
+    void* block = nullptr;
+    gbsph_bvh2d_node* node = nullptr;
+    uint32_t *key = nullptr, *val = nullptr, *visits = nullptr, *root = nullptr;
+    int32_t* parent = nullptr;
+    uint8_t *bits = nullptr, *bmax = nullptr, *smax = nullptr;
+    std::string last_error;
+};
+
+namespace {
+
+int ensure_lines(gbsph_bvh_lines_s* h, uint32_t n) {
+    if (n <= h->cap && h->block) return GBSPH_OK;
+    if (h->block) cudaFree(h->block);
+    h->block = nullptr;
+    h->cap = 0;
+    const size_t nn = 2 * (size_t)n, m = n;
+    const size_t nb = (m + BLK - 1) / BLK, ns = (m + SBLK - 1) / SBLK;
+    auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t bytes = al(nn * sizeof(gbsph_bvh2d_node)) + 3 * al(m * 4) + al(nn * 4) + al(m) + al(nb) + al(ns) + 256;
+    GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->block, bytes));
+    char* p = (char*)h->block;
+    h->node = (gbsph_bvh2d_node*)p;
+    p += al(nn * sizeof(gbsph_bvh2d_node));
+    h->key = (uint32_t*)p;
+    p += al(m * 4);
+    h->val = (uint32_t*)p;
+    p += al(m * 4);
+    h->visits = (uint32_t*)p;
+    p += al(m * 4);
+    h->parent = (int32_t*)p;
+    p += al(nn * 4);
+    h->bits = (uint8_t*)p;
+    p += al(m);
+    h->bmax = (uint8_t*)p;
+    p += al(nb);
+    h->smax = (uint8_t*)p;
+    p += al(ns);
+    h->root = (uint32_t*)p;
+    h->cap = n;
+    return GBSPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+GBSPH_API int gbsph_bvh_lines_create(gbsph_bvh_lines_t* out) {
+    if (!out) return GBSPH_ERR_ARGUMENT;
+    *out = nullptr;
+    gbsph_bvh_lines_s* h = new gbsph_bvh_lines_s();
+    int rc = cudaGetDevice(&h->device) == cudaSuccess ? GBSPH_OK : GBSPH_ERR_CUDA;
+    if (!rc) rc = gbsph_radix_sort_create(&h->sort);
+    if (rc) {
+        cudaGetLastError();
+        if (h->sort) gbsph_radix_sort_destroy(h->sort);
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_bvh_lines_destroy(gbsph_bvh_lines_t h) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    cudaSetDevice(h->device);
+    if (h->block) cudaFree(h->block);
+    if (h->sort) gbsph_radix_sort_destroy(h->sort);
+    delete h;
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_bvh_lines_compute(gbsph_bvh_lines_t h, const float* vertex, size_t n_vertices, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!vertex) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null buffer");
+    const size_t nl = n_vertices / 2;
+    if (nl < 2) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "a BVH needs at least 2 segments");
+    if (nl > SORT_MAX_KEYS - SORT_TILE) return fail(&h->last_error, GBSPH_ERR_TOO_LARGE, "too many segments");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    const uint32_t n = (uint32_t)nl, m = n - 1;
+    int rc = ensure_lines(h, n);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const float2* v2 = reinterpret_cast<const float2*>(vertex);
+    k_bvh_morton_lines<<<grid(n), BVH_THREADS, 0, s>>>(v2, n, h->key, h->val);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    rc = gbsph_radix_sort_compute(h->sort, h->key, h->val, n, n, 0, 32, stream);
+    if (rc) return fail(&h->last_error, rc, std::string("sort: ") + gbsph_radix_sort_last_error(h->sort));
+    const uint32_t nb = (m + BLK - 1) / BLK;
+    k_bvh_nodes<gbsph_bvh2d_node, 31><<<grid(m), BVH_THREADS, 0, s>>>(h->key, m, h->node, h->bits, h->bmax);
+    k_bvh_smax<<<(unsigned)((nb + 255) / 256 / (SBLK / BLK) + 1), 256, 0, s>>>(h->bmax, nb, h->smax);
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->root, 0, 4, s));
+    k_bvh_link<gbsph_bvh2d_node><<<grid(m), BVH_THREADS, 0, s>>>(h->bits, h->bmax, h->smax, (int)m, h->node, h->root);
+    k_bvh_leaves<gbsph_bvh2d_node><<<grid(n), BVH_THREADS, 0, s>>>(h->val, n, h->node);
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->parent, 0xFF, (2 * (size_t)n - 1) * 4, s));
+    k_bvh_parents<gbsph_bvh2d_node><<<grid(m), BVH_THREADS, 0, s>>>(h->node, m, h->parent, h->visits);
+    k_bvh_refit_lines<<<grid(n), BVH_THREADS, 0, s>>>(v2, n, h->node, h->parent, h->visits, h->root);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    h->n = n;
+    return GBSPH_OK;
+}
+
+GBSPH_API gbsph_bvh2d_node* gbsph_bvh_lines_get_node_buffer(gbsph_bvh_lines_t h, size_t* count) {
+    if (!h) return nullptr;
+    if (count) *count = h->n ? 2 * (size_t)h->n - 1 : 0;
+    return h->node;
+}
+
+GBSPH_API size_t gbsph_bvh_lines_get_node_count(gbsph_bvh_lines_t h) { return h && h->n ? 2 * (size_t)h->n - 1 : 0; }
+
+GBSPH_API int gbsph_bvh_lines_get_root_node(gbsph_bvh_lines_t h, uint32_t* root, void* stream) {
+    if (!h || !root) return GBSPH_ERR_ARGUMENT;
+    if (!h->root) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "no build yet");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize((cudaStream_t)stream));
+    GBSPH_CUDA_TRY(&h->last_error, cudaMemcpy(root, h->root, 4, cudaMemcpyDeviceToHost));
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_bvh_lines_sync_status(gbsph_bvh_lines_t h, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize((cudaStream_t)stream));
+    const int src = gbsph_radix_sort_sync_status(h->sort, stream);
+    if (src) return fail(&h->last_error, src, std::string("sort: ") + gbsph_radix_sort_last_error(h->sort));
+    return GBSPH_OK;
+}
+
+GBSPH_API const char* gbsph_bvh_lines_last_error(gbsph_bvh_lines_t h) { return h ? h->last_error.c_str() : "null handle"; }
+
+}  // extern "C"

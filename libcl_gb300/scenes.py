@@ -283,3 +283,29 @@ def lattice_soup(k: int = 100, seed: int = 22, size: float = 0.002):
     v = np.ones((3 * n, 4), np.float32)
     v[:, :3] = (c[:, None, :] + d).reshape(3 * n, 3)
     return v, np.arange(3 * n, dtype=np.uint32)
+
+
+def segment_soup(n: int, seed: int = 23, extent: float = 65000.0, size: float = 20.0):
+    """n independent 2D line segments: midpoints uniform in [0, extent)^2 (SplitMix64), ends
+    within +-size of the midpoint, in the integer pixel space oclBvhLines keys on. Returns
+    vertex float32 [2n, 2] (two vertices per segment)."""
+    rng = SplitMix64(seed)
+    c = rng.uniform(2 * n).reshape(n, 1, 2) * extent + size
+    d = (rng.uniform(2 * n).reshape(n, 1, 2) * 2.0 - 1.0) * size
+    v = np.concatenate([c - d, c + d], axis=1)
+    return v.reshape(2 * n, 2).astype(np.float32)
+
+
+def segment_lattice(k: int = 1000, seed: int = 24):
+    """k^2 short segments whose midpoints sit on distinct integer points of a k x k lattice
+    (spacing 64, so their Morton keys are distinct for k <= 1024), shuffled. Returns vertex
+    float32 [2 k^2, 2]."""
+    rng = SplitMix64(seed)
+    n = k * k
+    iy, ix = np.meshgrid(np.arange(k), np.arange(k), indexing="ij")
+    c = np.stack([ix.ravel(), iy.ravel()], axis=1).astype(np.float64) * 64.0 + 16.5
+    c = c[np.argsort(rng.next_u64(n), kind="stable")]
+    d = (rng.uniform(2 * n).reshape(n, 2) * 2.0 - 1.0) * 8.0
+    v = np.stack([c - d, c + d], axis=1)
+    return v.reshape(2 * n, 2).astype(np.float32)
+

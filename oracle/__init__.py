@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
             "orc_adjoint_f64": (C.c_int, [P, P, P, U, P, U, U, P, P, P, P, P]),
             "orc_adjoint_states_f64": (C.c_int, [P, P, P, U, P, U, P, P, P, P, P]),
             "orc_bvh_build": (C.c_int, [P, U, P, U, P, P, P, P, P]),
+            "orc_bvh_lines_build": (C.c_int, [P, U, P, P, P, P]),
             "orc_bvh_collide": (None, [P, P, P, P, U, P, U, P, P]),
         }
         for name, (res, args) in sig.items():
@@ -299,6 +300,26 @@ def bvh_build(vertex: np.ndarray, index: np.ndarray, box: np.ndarray, root: int 
     sk = np.empty(n, np.uint32)
     sv = np.empty(n, np.uint32)
     rc = lib().orc_bvh_build(_p(vertex), vertex.shape[0], _p(index), n, _p(box), _p(nodes), _p(r), _p(sk), _p(sv))
+    assert rc == 0, rc
+    return nodes, int(r[0]), sk, sv
+
+
+BVH2D_NODE_DTYPE = np.dtype([("bbMin", np.float32, 2), ("bbMax", np.float32, 2), ("left", np.int32),
+                             ("right", np.int32), ("bit", np.uint32), ("trav", np.uint32)])
+
+
+def bvh_lines_build(vertex: np.ndarray, root: int = 0):
+    """The reference's 2D segment BVH build (oclBvhLines::compute) on a host float32 [V, 2]
+    array (two vertices per segment). Returns (nodes [2n - 1], root, sorted keys, sorted
+    segment ids)."""
+    vertex = np.ascontiguousarray(vertex, np.float32)
+    n = vertex.shape[0] // 2
+    vertex = np.ascontiguousarray(vertex[:2 * n])
+    nodes = np.zeros(2 * n - 1, BVH2D_NODE_DTYPE)
+    r = np.array([root], np.uint32)
+    sk = np.empty(n, np.uint32)
+    sv = np.empty(n, np.uint32)
+    rc = lib().orc_bvh_lines_build(_p(vertex), n, _p(nodes), _p(r), _p(sk), _p(sv))
     assert rc == 0, rc
     return nodes, int(r[0]), sk, sv
 

@@ -1,4 +1,5 @@
-// oraclebvh.cpp -- CPU restatement of the reference's triangle-mesh BVH build.
+// oraclebvh.cpp -- CPU restatement of the reference's BVH builds (triangle mesh and 2D line
+// segments) and of its particle-vs-mesh collision.
 //
 // TEST INFRASTRUCTURE ONLY, like oracle3d.cpp: nothing in the product links or calls it.
 // It follows oclBvhTrimesh::compute (libCL/geom/oclBvhTrimesh.cpp:56-143) and the kernels of
@@ -175,6 +176,157 @@ int orc_bvh_build(const float* vertex, uint32_t nv, const uint32_t* index, uint3
             for (int c = 0; c < 4; c++) {
                 nd.bbMin[c] = clmin(l.bbMin[c], r.bbMin[c]);
                 nd.bbMax[c] = clmax(l.bbMax[c], r.bbMax[c]);
+            }
+        }
+    }
+    if (sorted_keys) std::memcpy(sorted_keys, sk.data(), 4 * (size_t)n);
+    if (sorted_vals) std::memcpy(sorted_vals, sv.data(), 4 * (size_t)n);
+    return 0;
+}
+
+}  // extern "C"
+
+// ---- oclBvhLines (libCL/geom/oclBvhLines.cpp:48-115, libCL/geom/oclBvhLines.cl:27-245) ---------
+namespace {
+
+uint32_t code16(uint32_t x) {  // clMorton's interleave, libCL/geom/oclBvhLines.cl:35-52
+    x &= 0x0000ffffu;
+    x |= x << 8;
+    x &= 0x00ff00ffu;
+    x |= x << 4;
+    x &= 0x0f0f0f0fu;
+    x |= x << 2;
+    x &= 0x33333333u;
+    x |= x << 1;
+    x &= 0x55555555u;
+    return x;
+}
+
+void init_node2(gbsph_bvh2d_node& nd, int32_t l, int32_t r, uint32_t bit) {
+    nd.bbMin[0] = nd.bbMin[1] = FLT_MAX;
+    nd.bbMax[0] = nd.bbMax[1] = -FLT_MAX;
+    nd.left = l;
+    nd.right = r;
+    nd.bit = bit;
+    nd.trav = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// One build over n segments. vertex: float2[2 n]; nodes: [2n - 1]; root: in/out (kept across
+// builds, as mRootNode). Returns 0, -1 for n < 2, -2 if a descent does not reach a leaf.
+int orc_bvh_lines_build(const float* vertex, uint32_t n, gbsph_bvh2d_node* nodes, uint32_t* root,
+                        uint32_t* sorted_keys, uint32_t* sorted_vals) {
+    if (n < 2) return -1;
+    // clMorton (:27-55): midpoint 0.5 * (v0 + v1), truncated, 16 bits per axis interleaved
+    std::vector<uint32_t> key(n), val(n);
+    for (uint32_t g = 0; g < n; g++) {
+        const float cx = 0.5f * (vertex[4 * (size_t)g] + vertex[4 * (size_t)g + 2]);
+        const float cy = 0.5f * (vertex[4 * (size_t)g + 1] + vertex[4 * (size_t)g + 3]);
+        key[g] = code16(to_uint(cx)) | (code16(to_uint(cy)) << 1);
+        val[g] = g;
+    }
+    // oclRadixSort on bits [0, 32): a stable sort
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+    std::vector<uint32_t> sk(n), sv(n);
+    for (uint32_t i = 0; i < n; i++) {
+        sk[i] = key[order[i]];
+        sv[i] = val[order[i]];
+    }
+    const uint32_t m = n - 1;
+    // clCreateNodes (:71-95): highest differing bit, 31 down to 0
+    for (uint32_t i = 0; i < m; i++) {
+        uint32_t bit = 0;
+        for (int b = 31; b >= 0; b--)
+            if (((sk[i] >> b) & 1u) != ((sk[i + 1] >> b) & 1u)) {
+                bit = (uint32_t)b;
+                break;
+            }
+        init_node2(nodes[i], -1, -1, bit);
+    }
+    // clLinkNodes (:97-151)
+    for (uint32_t g = 0; g < m; g++) {
+        const uint32_t bit = nodes[g].bit;
+        int left = -1, right = -1;
+        for (int i = (int)g - 1; i >= 0; i--)
+            if (nodes[i].bit > bit) {
+                left = i;
+                break;
+            }
+        for (uint32_t i = g + 1; i < m; i++)
+            if (nodes[i].bit > bit) {
+                right = (int)i;
+                break;
+            }
+        if (left != -1 || right != -1) {
+            if (right == -1) nodes[left].right = (int32_t)g;
+            else if (left == -1) nodes[right].left = (int32_t)g;
+            else if (nodes[left].bit < nodes[right].bit) nodes[left].right = (int32_t)g;
+            else nodes[right].left = (int32_t)g;
+        } else {
+            *root = g;
+        }
+    }
+    // clCreateLeaves (:153-184): the leaf's box is left to clComputeAABBs
+    const uint32_t ls = n - 1;
+    for (uint32_t g = 0; g < n; g++) {
+        gbsph_bvh2d_node& L = nodes[ls + g];
+        L.bit = sv[g];
+        L.left = L.right = 0;
+        L.trav = 0;
+        if (g == 0) {
+            nodes[0].left = (int32_t)(ls + g);
+            continue;
+        }
+        if (g == ls) {
+            nodes[ls - 1].right = (int32_t)(ls + g);
+            continue;
+        }
+        if (nodes[g].left == -1) nodes[g].left = (int32_t)(g + ls);
+        else if (nodes[g - 1].right == -1) nodes[g - 1].right = (int32_t)(g + ls);
+    }
+    // clComputeAABBs (:186-245): per segment, step down by node index until a leaf, box it,
+    // then climb: the first visitor leaves trav = 2 and stops; the second swaps 2 for 3 and
+    // computes the node's box from its children
+    for (uint32_t g = 0; g < n; g++) {
+        std::vector<uint32_t> stack;
+        stack.push_back(*root);
+        for (;;) {
+            const gbsph_bvh2d_node& nd = nodes[stack.back()];
+            stack.push_back(stack.back() >= g ? (uint32_t)nd.left : (uint32_t)nd.right);
+            if (stack.size() > 2 * (size_t)n) return -2;
+            gbsph_bvh2d_node& c = nodes[stack.back()];
+            if (c.left == c.right) {
+                const uint32_t seg = c.bit;
+                float mn[2] = {FLT_MAX, FLT_MAX}, mx[2] = {-FLT_MAX, -FLT_MAX};
+                for (int k = 0; k < 2; k++)
+                    for (int a = 0; a < 2; a++) {
+                        const float v = vertex[4 * (size_t)seg + 2 * k + a];
+                        mn[a] = clmin(mn[a], v);
+                        mx[a] = clmax(mx[a], v);
+                    }
+                std::memcpy(c.bbMin, mn, 8);
+                std::memcpy(c.bbMax, mx, 8);
+                break;
+            }
+        }
+        size_t top = stack.size() - 1;
+        while (top--) {
+            gbsph_bvh2d_node& nd = nodes[stack[top]];
+            if (nd.trav == 0) {
+                nd.trav = 2;
+                break;
+            }
+            nd.trav = 3;
+            const gbsph_bvh2d_node& l = nodes[nd.left];
+            const gbsph_bvh2d_node& r = nodes[nd.right];
+            for (int a = 0; a < 2; a++) {
+                nd.bbMin[a] = clmin(l.bbMin[a], r.bbMin[a]);
+                nd.bbMax[a] = clmax(l.bbMax[a], r.bbMax[a]);
             }
         }
     }

@@ -1,12 +1,13 @@
-"""GPU parity of the triangle-mesh BVH (gbsph_bvh_*) against the oracle's restatement of
-oclBvhTrimesh: every node (boxes, children, split bit or triangle, visit flag), the root and
-the accumulated global box bit-exact."""
+"""GPU parity of the triangle-mesh BVH (gbsph_bvh_*) and of the 2D segment BVH
+(gbsph_bvh_lines_*) against the oracle's restatements of oclBvhTrimesh and oclBvhLines: every
+node (boxes, children, split bit or primitive, visit flag), the root and (triangles) the
+accumulated global box bit-exact."""
 import numpy as np
 import pytest
 
 import oracle
-from libcl_gb300 import ERR_ARGUMENT, ERR_DEVICE_RANGE, BvhTrimesh
-from libcl_gb300.scenes import lattice_soup, sphere_mesh, triangle_soup
+from libcl_gb300 import ERR_ARGUMENT, ERR_DEVICE_RANGE, BvhLines, BvhTrimesh
+from libcl_gb300.scenes import lattice_soup, segment_lattice, segment_soup, sphere_mesh, triangle_soup
 
 pytestmark = pytest.mark.gpu
 
@@ -138,3 +139,47 @@ def test_bvh_collide_bit_exact(cuda):
     assert hit.sum() > 1000, hit.sum()
     for g, r, name in ((dpos, rp, "position"), (dvel, rv, "velocity"), (dfrc, rf, "force")):
         np.testing.assert_array_equal(g.cpu().numpy().view(np.uint32), r.view(np.uint32), err_msg=name)
+
+
+def lines_build_both(b, v, root=0):
+    import torch
+    b.compute(torch.from_numpy(v).cuda())
+    assert b.sync_status() == 0
+    o, root, sk, _ = oracle.bvh_lines_build(v, root)
+    g = b.getNodeBuffer().cpu().numpy().view(oracle.BVH2D_NODE_DTYPE).ravel()
+    return g, o, root, sk
+
+
+@pytest.mark.parametrize("scene", ["soup_20k", "lattice_1m"])
+def test_bvh_lines_bit_exact(cuda, scene):
+    v = segment_soup(20000) if scene == "soup_20k" else segment_lattice(1000)
+    b = BvhLines()
+    g, o, root, sk = lines_build_both(b, v)
+    assert len(np.unique(sk)) == sk.size
+    assert b.getNodeCount() == 2 * (v.shape[0] // 2) - 1
+    assert b.getRootNode() == root
+    assert_same(g, o)
+
+
+def test_bvh_lines_rebuild_and_repeated_keys(cuda):
+    """Two builds on one handle (the second smaller, with many repeated keys: 4,000 segments
+    whose midpoints fall on a 40 x 40 pixel square): the first bit-exact; the second's links,
+    split bits, leaves and root as in the oracle's sequential run."""
+    b = BvhLines()
+    g, o, root, sk = lines_build_both(b, segment_soup(8000, seed=5))
+    assert_same(g, o)
+    v2 = segment_soup(4000, seed=6, extent=40.0, size=2.0)
+    g, o, root, sk = lines_build_both(b, v2, root)
+    assert len(np.unique(sk)) < sk.size
+    for f in ("left", "right", "bit"):
+        np.testing.assert_array_equal(g[f], o[f], err_msg=f)
+    assert b.getRootNode() == root
+
+
+def test_bvh_lines_errors(cuda):
+    import torch
+    b = BvhLines()
+    with pytest.raises(Exception) as e:
+        b.compute(torch.zeros(3, 2, device="cuda"))  # one segment (the odd vertex is ignored)
+    assert e.value.status == ERR_ARGUMENT
+
