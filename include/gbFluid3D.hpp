@@ -6,6 +6,10 @@
 //   oclRadixSort             (libCL/sort/oclRadixSort.h:22-49)                     -> gbRadixSort
 //   oclFluid3D + srtEvent    (libCL/phys/oclFluid3D.h:21-123, libCL/oclProgram.h:104-116)
 //                                                                                  -> gbFluid3D + srtEvent
+//   oclImage2D               (libCL/oclImage2D.h, an RGBA float image)           -> gbImage2D
+//   oclFluid2D               (libCL/phys/oclFluid2D.h:22-79)                      -> gbFluid2D
+//   oclBvhTrimesh            (libCL/geom/oclBvhTrimesh.h:20-84)                   -> gbBvhTrimesh
+//   oclBvhLines              (libCL/geom/oclBvhLines.h:20-77)                     -> gbBvhLines
 // Same method names and meanings: construct, compile(), setParticleCount(), set/get buffers,
 // getParameters(), addEventHandler(EVT_INTEGRATE), compute(device), map()/unmap() to read
 // results. Methods return 1/true on success and 0/false on failure like the reference; the
@@ -232,3 +236,167 @@ class gbFluid3D {
     srtEvent* mHandler = nullptr;
     gbDevice* mDevice = nullptr;
 };
+
+// A device RGBA float image (the wall mask oclFluid2D::computeBorder reads).
+class gbImage2D {
+   public:
+    gbImage2D(gbContext&, const char* name) : mName(name) {}
+    ~gbImage2D() {
+        if (mPtr) cudaFree(mPtr);
+    }
+    gbImage2D(const gbImage2D&) = delete;
+    gbImage2D& operator=(const gbImage2D&) = delete;
+    bool create(int width, int height) {
+        if (mPtr) cudaFree(mPtr);
+        mPtr = nullptr;
+        gbStatus() = cudaMalloc(&mPtr, (size_t)width * height * 16) == cudaSuccess ? GBSPH_OK : GBSPH_ERR_OUT_OF_MEMORY;
+        if (gbStatus() != GBSPH_OK) return false;
+        cudaMemset(mPtr, 0, (size_t)width * height * 16);
+        mW = width;
+        mH = height;
+        return true;
+    }
+    // Uploads width * height RGBA float pixels.
+    bool write(const float* rgba) {
+        return cudaMemcpy(mPtr, rgba, (size_t)mW * mH * 16, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    int getImageWidth() const { return mW; }
+    int getImageHeight() const { return mH; }
+    const float* devicePtr() const { return mPtr; }
+
+   private:
+    std::string mName;
+    float* mPtr = nullptr;
+    int mW = 0, mH = 0;
+};
+
+// oclFluid2D: the 2D relaxation model. Same calls: compile(), setParticleCount(),
+// setStateBuffer() / getStateBuffer() (Particle records, 24 bytes), computeBorder(image),
+// getParameters(), compute(device).
+class gbFluid2D {
+   public:
+    typedef gbsph_fluid2d_params Params;
+    typedef gbsph_particle2d Particle;
+    static constexpr size_t cLocalSize = 256;
+
+    explicit gbFluid2D(gbContext& ctx) : mState(ctx, "bfParticle") {
+        gbStatus() = gbsph_fluid2d_create(&mH);
+        rewrap();
+    }
+    ~gbFluid2D() {
+        if (mH) gbsph_fluid2d_destroy(mH);
+    }
+    gbFluid2D(const gbFluid2D&) = delete;
+    gbFluid2D& operator=(const gbFluid2D&) = delete;
+
+    int compile() { return ok(gbsph_fluid2d_compile(mH)); }
+    int compute(gbDevice& dev) { return ok(gbsph_fluid2d_compute(mH, dev.getQueue())); }
+    void setParticleCount(size_t n) {
+        ok(gbsph_fluid2d_set_particle_count(mH, n));
+        mUser = nullptr;
+        rewrap();
+    }
+    size_t getParticleCount() { return gbsph_fluid2d_get_particle_count(mH); }
+    int setStateBuffer(gbBuffer* b) {
+        const int r = ok(gbsph_fluid2d_set_state_buffer(mH, b->devicePtr(), b->count<Particle>()));
+        if (r) mUser = b;
+        return r;
+    }
+    gbBuffer* getStateBuffer() { return mUser ? mUser : &mState; }
+    void computeBorder(gbImage2D* image) {
+        ok(gbsph_fluid2d_compute_border(mH, image->devicePtr(), image->getImageWidth(), image->getImageHeight(),
+                                        nullptr));
+    }
+    Params& getParameters() { return *gbsph_fluid2d_get_params(mH); }
+    const char* lastError() const { return gbsph_fluid2d_last_error(mH); }
+    gbsph_fluid2d_t handle() const { return mH; }
+
+   private:
+    int ok(int status) {
+        gbStatus() = status;
+        return status == GBSPH_OK;
+    }
+    void rewrap() {
+        size_t count = 0;
+        void* p = mH ? gbsph_fluid2d_get_buffer(mH, GBSPH2D_BUF_STATE, &count) : nullptr;
+        mState.wrap(p, count * sizeof(Particle));
+        mState.setOwner(this);
+    }
+    gbsph_fluid2d_t mH = nullptr;
+    gbBuffer mState;
+    gbBuffer* mUser = nullptr;
+};
+
+// oclBvhTrimesh: compute(device, vertex float4 buffer, index uint buffer), then the node
+// buffer (BVHNode records, 48 bytes), node count and root.
+class gbBvhTrimesh {
+   public:
+    typedef gbsph_bvh_node BVHNode;
+    explicit gbBvhTrimesh(gbContext& ctx) : mNodes(ctx, "bfBvhNode") { gbStatus() = gbsph_bvh_create(&mH); }
+    ~gbBvhTrimesh() {
+        if (mH) gbsph_bvh_destroy(mH);
+    }
+    gbBvhTrimesh(const gbBvhTrimesh&) = delete;
+    gbBvhTrimesh& operator=(const gbBvhTrimesh&) = delete;
+    int compute(gbDevice& dev, gbBuffer& vertex, gbBuffer& index) {
+        mDevice = &dev;
+        gbStatus() = gbsph_bvh_compute(mH, (const float*)vertex.devicePtr(), vertex.count<float>() / 4,
+                                       (const uint32_t*)index.devicePtr(), index.count<uint32_t>(), dev.getQueue());
+        size_t count = 0;
+        void* p = gbsph_bvh_get_node_buffer(mH, &count);
+        mNodes.wrap(p, count * sizeof(BVHNode));
+        mNodes.setOwner(this);
+        return gbStatus() == GBSPH_OK;
+    }
+    gbBuffer& getNodeBuffer() { return mNodes; }
+    uint32_t getNodeCount() { return (uint32_t)gbsph_bvh_get_node_count(mH); }
+    uint32_t getRootNode() {
+        uint32_t r = 0;
+        gbStatus() = gbsph_bvh_get_root_node(mH, &r, mDevice ? mDevice->getQueue() : nullptr);
+        return r;
+    }
+    const char* lastError() const { return gbsph_bvh_last_error(mH); }
+    gbsph_bvh_t handle() const { return mH; }
+
+   private:
+    gbsph_bvh_t mH = nullptr;
+    gbBuffer mNodes;
+    gbDevice* mDevice = nullptr;
+};
+
+// oclBvhLines: compute(device, vertex float2 buffer, two vertices per segment), then the node
+// buffer (BVHNode records, 32 bytes), node count and root.
+class gbBvhLines {
+   public:
+    typedef gbsph_bvh2d_node BVHNode;
+    explicit gbBvhLines(gbContext& ctx) : mNodes(ctx, "bfBvhNode") { gbStatus() = gbsph_bvh_lines_create(&mH); }
+    ~gbBvhLines() {
+        if (mH) gbsph_bvh_lines_destroy(mH);
+    }
+    gbBvhLines(const gbBvhLines&) = delete;
+    gbBvhLines& operator=(const gbBvhLines&) = delete;
+    int compute(gbDevice& dev, gbBuffer& vertex) {
+        mDevice = &dev;
+        gbStatus() = gbsph_bvh_lines_compute(mH, (const float*)vertex.devicePtr(), vertex.count<float>() / 2,
+                                             dev.getQueue());
+        size_t count = 0;
+        void* p = gbsph_bvh_lines_get_node_buffer(mH, &count);
+        mNodes.wrap(p, count * sizeof(BVHNode));
+        mNodes.setOwner(this);
+        return gbStatus() == GBSPH_OK;
+    }
+    gbBuffer& getNodeBuffer() { return mNodes; }
+    uint32_t getNodeCount() { return (uint32_t)gbsph_bvh_lines_get_node_count(mH); }
+    uint32_t getRootNode() {
+        uint32_t r = 0;
+        gbStatus() = gbsph_bvh_lines_get_root_node(mH, &r, mDevice ? mDevice->getQueue() : nullptr);
+        return r;
+    }
+    const char* lastError() const { return gbsph_bvh_lines_last_error(mH); }
+
+   private:
+    gbsph_bvh_lines_t mH = nullptr;
+    gbBuffer mNodes;
+    gbDevice* mDevice = nullptr;
+};
+

@@ -1,7 +1,9 @@
 // C++ drop-in smoke test of the class surface, following the reference's driver
 // (libCL/TEST/main.cpp): testRadixSort (:133-181), testFluid3D0 (:188-240) and
 // testFluid3D1 with an EVT_INTEGRATE handler (:246-343), with fixed step counts instead of
-// 7 seconds of wall clock, and with assertions the reference does not make.
+// 7 seconds of wall clock, and with assertions the reference does not make; then the 2D
+// model and the two BVH builds through their classes (the reference's driver has no test
+// for them).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -123,9 +125,116 @@ static int testFluid3D1(gbContext& ctx) {
     return 0;
 }
 
+// oclFluid2D: compile, a dam-break block of particles in the default container, a border
+// image with a wall column, 20 steps; positions stay finite and inside the container.
+static int testFluid2D(gbContext& ctx) {
+    gbDevice& dev = ctx.getDevice(0);
+    gbFluid2D fluid(ctx);
+    CHECK(fluid.compile());
+    fluid.setParticleCount(4096);
+    gbFluid2D::Params& p = fluid.getParameters();
+    gbBuffer* st = fluid.getStateBuffer();
+    CHECK(st->count<gbFluid2D::Particle>() == 4096);
+    CHECK(st->map(gbBuffer::MAP_WRITE));
+    for (int i = 0; i < 4096; i++) {
+        gbFluid2D::Particle& q = st->ptr<gbFluid2D::Particle>()[i];
+        q.pos[0] = 1.0f + (i % 64) * 0.5f * p.h;  // a 64 x 64 block in the lower left of the container
+        q.pos[1] = 1.0f + (i / 64) * 0.5f * p.h;
+        q.vel[0] = q.vel[1] = 0.0f;
+        q.mass = p.particleMass;
+        q.unused = 0.0f;
+    }
+    CHECK(st->unmap());
+    gbImage2D wall(ctx, "imBorder");
+    CHECK(wall.create(256, 256));
+    std::vector<float> img(256 * 256 * 4, 0.0f);
+    for (int y = 0; y < 256; y++) img[4 * (y * 256 + 200) + 3] = 1.0f;  // a wall column at x = 200
+    CHECK(wall.write(img.data()));
+    fluid.computeBorder(&wall);
+    CHECK(gbStatus() == GBSPH_OK);
+    for (int i = 0; i < 20; i++) CHECK(fluid.compute(dev));
+    cudaDeviceSynchronize();
+    CHECK(st->map(gbBuffer::MAP_READ));
+    for (int i = 0; i < 4096; i++) {
+        const gbFluid2D::Particle& q = st->ptr<gbFluid2D::Particle>()[i];
+        CHECK(std::isfinite(q.pos[0]) && std::isfinite(q.pos[1]));
+    }
+    std::printf("testFluid2D completed\n");
+    return 0;
+}
+
+// oclBvhTrimesh and oclBvhLines: build over a few primitives; 2n - 1 nodes, a root among the
+// internal nodes whose box contains every primitive.
+static int testBvh(gbContext& ctx) {
+    gbDevice& dev = ctx.getDevice(0);
+    const int n = 64;
+    gbBuffer vtx(ctx, "bfVertex"), idx(ctx, "bfIndex");
+    CHECK(vtx.create<float>(4 * 3 * n) && idx.create<unsigned>(3 * n));
+    vtx.map(gbBuffer::MAP_WRITE);
+    idx.map(gbBuffer::MAP_WRITE);
+    unsigned s = 3;
+    for (int t = 0; t < n; t++) {
+        const float cx = (float)(lcg(s) >> 8) / (1 << 24), cy = (float)(lcg(s) >> 8) / (1 << 24),
+                    cz = (float)(lcg(s) >> 8) / (1 << 24);
+        for (int k = 0; k < 3; k++) {
+            float* v = vtx.ptr<float>() + 4 * (3 * t + k);
+            v[0] = cx + 0.01f * k;
+            v[1] = cy + 0.01f * (k == 1);
+            v[2] = cz;
+            v[3] = 1.0f;
+            idx.ptr<unsigned>()[3 * t + k] = 3 * t + k;
+        }
+    }
+    CHECK(vtx.unmap() && idx.unmap());
+    gbBvhTrimesh tri(ctx);
+    CHECK(tri.compute(dev, vtx, idx));
+    CHECK(tri.getNodeCount() == 2 * n - 1);
+    const uint32_t root = tri.getRootNode();
+    CHECK(root < (uint32_t)(n - 1));
+    gbBuffer& nodes = tri.getNodeBuffer();
+    CHECK(nodes.count<gbBvhTrimesh::BVHNode>() == (size_t)(2 * n - 1));
+    CHECK(nodes.map(gbBuffer::MAP_READ));
+    const gbBvhTrimesh::BVHNode& r = nodes.ptr<gbBvhTrimesh::BVHNode>()[root];
+    CHECK(r.trav == 2);
+    vtx.map(gbBuffer::MAP_READ);
+    for (int i = 0; i < 3 * n; i++)
+        for (int c = 0; c < 3; c++) {
+            const float v = vtx.ptr<float>()[4 * i + c];
+            CHECK(v >= r.bbMin[c] && v <= r.bbMax[c]);
+        }
+
+    gbBuffer seg(ctx, "bfSegment");
+    CHECK(seg.create<float>(2 * 2 * n));
+    seg.map(gbBuffer::MAP_WRITE);
+    for (int i = 0; i < n; i++) {
+        float* v = seg.ptr<float>() + 4 * i;
+        v[0] = (float)(lcg(s) >> 16);
+        v[1] = (float)(lcg(s) >> 16);
+        v[2] = v[0] + 3.0f;
+        v[3] = v[1] + 5.0f;
+    }
+    CHECK(seg.unmap());
+    gbBvhLines lines(ctx);
+    CHECK(lines.compute(dev, seg));
+    CHECK(lines.getNodeCount() == 2 * n - 1);
+    const uint32_t lroot = lines.getRootNode();
+    CHECK(lroot < (uint32_t)(n - 1));
+    gbBuffer& lnodes = lines.getNodeBuffer();
+    CHECK(lnodes.map(gbBuffer::MAP_READ));
+    seg.map(gbBuffer::MAP_READ);
+    const gbBvhLines::BVHNode& lr = lnodes.ptr<gbBvhLines::BVHNode>()[lroot];
+    CHECK(lr.trav == 3);
+    for (int i = 0; i < 2 * n; i++) {
+        const float* v = seg.ptr<float>() + 2 * i;
+        CHECK(v[0] >= lr.bbMin[0] && v[0] <= lr.bbMax[0] && v[1] >= lr.bbMin[1] && v[1] <= lr.bbMax[1]);
+    }
+    std::printf("testBvh completed\n");
+    return 0;
+}
+
 int main() {
     gbContext ctx(0);
-    if (testRadixSort(ctx) || testFluid3D0(ctx) || testFluid3D1(ctx)) return 1;
+    if (testRadixSort(ctx) || testFluid3D0(ctx) || testFluid3D1(ctx) || testFluid2D(ctx) || testBvh(ctx)) return 1;
     std::printf("OK\n");
     return 0;
 }
