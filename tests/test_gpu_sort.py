@@ -177,3 +177,43 @@ def test_sort_16m_pairs(cuda, dist):
     k, v = _run(RadixSort(), keys, vals, *bits)
     ek, ev = _expected(keys, vals, *bits)
     assert np.array_equal(k, ek) and np.array_equal(v, ev)
+
+
+MAX_KEYS = (1 << 30) - 1 - 4096  # the largest sortable count (the C ABI refuses one more)
+
+
+def test_sort_maximum_size(cuda):
+    """The largest accepted sort: 1,073,737,727 random 32-bit pairs, checked on the device
+    in 64M-key slices: keys ascending, each output value the input position of its key
+    (orig[val] == key), equal keys in input order (stability), and the values a
+    permutation. One more key is refused with GBSPH_ERR_TOO_LARGE before any device work."""
+    import torch
+    from libcl_gb300 import ERR_TOO_LARGE
+    n = MAX_KEYS
+    g = torch.Generator(device="cuda").manual_seed(7)
+    keys = torch.randint(-(1 << 31), 1 << 31, (n,), dtype=torch.int32, device="cuda", generator=g)
+    orig = keys.clone()
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    sorter = RadixSort()
+    sorter.compute(keys, vals, 0, 32)
+    torch.cuda.synchronize()
+    assert sorter.sync_status() == OK
+    step = 1 << 26
+    mask = 0xFFFFFFFF
+    for a in range(0, n, step):
+        b = min(n, a + step + 1)  # one key of overlap with the next slice
+        k = keys[a:b].to(torch.int64) & mask
+        v = vals[a:b].to(torch.int64)
+        assert bool((k[1:] >= k[:-1]).all()), f"not sorted in [{a}, {b})"
+        eq = k[1:] == k[:-1]
+        assert bool((v[1:][eq] > v[:-1][eq]).all()), f"not stable in [{a}, {b})"
+        assert bool((orig[vals[a:b].long()] == keys[a:b]).all()), f"value does not index its key in [{a}, {b})"
+        del k, v, eq
+    vs, _ = torch.sort(vals)
+    for a in range(0, n, step):
+        b = min(n, a + step)
+        assert bool((vs[a:b] == torch.arange(a, b, dtype=torch.int32, device="cuda")).all())
+    del vs, keys, orig, vals
+    torch.cuda.empty_cache()
+    lib = sorter._lib
+    assert lib.gbsph_radix_sort_compute(sorter._h, None, None, n + 1, n + 1, 0, 32, None) == ERR_TOO_LARGE
