@@ -387,6 +387,111 @@ def extra_bvh_lines(stream) -> dict:
             "cpu_reference_port_ms": cpu_s * 1e3, "cpu_cores": 1}
 
 
+def profile_suite(stream) -> None:
+    """One untimed pass over every hot path, sized for a per-kernel ncu capture (about 1 GB on
+    the device at a time): 3 fused steps of the 1M block collapse; the 16M uniform and Morton
+    sorts with cell bounds; 2 steps of a 32-scene batch; a 10-step adjoint (checkpoint every
+    5) of the 65,536-particle block; the 1M-triangle and 1M-segment BVH builds and a collision
+    pass; 3 steps of the 2D dam break (dims = 2) and of the 2D relaxation model."""
+    import torch
+    from libcl_gb300 import (BUF_FORCE, BUF_POSITION, BUF_VELOCITY, Adjoint3D, Batch3D, BvhLines, BvhTrimesh,
+                             Fluid2D, Fluid3D, RadixSort, default_params)
+    from libcl_gb300.scenes import (SplitMix64, batched_ensemble, block_collapse_3d, dam_break_2d,
+                                    differentiable_block, lattice_soup, segment_lattice, sphere_mesh)
+
+    def done():
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+
+    f = Fluid3D()
+    load_scene(f, block_collapse_3d())
+    for _ in range(3):
+        f.compute(stream)
+    assert f.sync_status() == 0
+    del f
+    done()
+    n = 1 << 24
+    rng = SplitMix64(3)
+    keys = torch.from_numpy((rng.next_u64(n) >> np.uint64(32)).astype(np.uint32).view(np.int32)).cuda()
+    vals = torch.arange(n, dtype=torch.int32, device="cuda")
+    s = RadixSort()
+    s.compute(keys, vals, 0, 32, stream)
+    keys.random_(0, 1 << 22)
+    s.compute(keys, vals, 0, 24, stream)
+    cs = torch.empty(1 << 22, dtype=torch.int32, device="cuda")
+    ce = torch.empty(1 << 22, dtype=torch.int32, device="cuda")
+    s.cell_bounds(keys, cs, ce, stream)
+    assert s.sync_status() == 0
+    del keys, vals, cs, ce, s
+    done()
+    b = batched_ensemble(n_scenes=32)
+    bt = Batch3D()
+    bt.set_scenes(b.shared, b.descs)
+    bt.buffer(BUF_POSITION).copy_(torch.from_numpy(b.pos))
+    bt.buffer(BUF_VELOCITY).zero_()
+    bt.buffer(BUF_FORCE).zero_()
+    for _ in range(2):
+        bt.compute(stream)
+    assert bt.sync_status() == 0
+    del bt
+    done()
+    sc = differentiable_block()
+    f = Fluid3D()
+    load_scene(f, sc)
+    adj = Adjoint3D(f, 10, 5)
+    gpos = torch.full((sc.n, 4), 1e-6, dtype=torch.float32, device="cuda")
+    gp0, gv0 = torch.empty_like(gpos), torch.empty_like(gpos)
+    gpar = torch.empty(2, dtype=torch.float64, device="cuda")
+    adj.forward(stream)
+    adj.backward_raw(gpos, None, gp0, gv0, gpar, stream)
+    assert f.sync_status() == 0
+    del adj, f
+    done()
+    v, idx = lattice_soup(100)
+    bv = BvhTrimesh()
+    bv.compute(torch.from_numpy(v).cuda(), torch.from_numpy(idx.view(np.int32)).cuda(), stream)
+    sv, si = sphere_mesh(24, 48)
+    dsv, dsi = torch.from_numpy(sv).cuda(), torch.from_numpy(si.view(np.int32)).cuda()
+    bv.compute(dsv, dsi, stream)
+    npart = 20000
+    d = rng.normal(3 * npart).reshape(npart, 3)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pos = np.zeros((npart, 4), np.float32)
+    vel = np.zeros((npart, 4), np.float32)
+    pos[:, :3] = 1.0 + d * 0.505
+    vel[:, :3] = -d * 2.0
+    dp, dvl = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
+    bv.collide(default_params(), dp, dvl, torch.zeros_like(dp), dsv, dsi, stream)
+    assert bv.sync_status() == 0
+    bl = BvhLines()
+    bl.compute(torch.from_numpy(segment_lattice(1000)).cuda(), stream)
+    assert bl.sync_status() == 0
+    del bv, bl
+    done()
+    f = Fluid3D()
+    load_scene(f, dam_break_2d())
+    for _ in range(3):
+        f.compute(stream)
+    assert f.sync_status() == 0
+    del f
+    g = Fluid2D()
+    g.compile()
+    m = g.getParticleCount()
+    st = np.zeros((m, 6), np.float32)
+    side = int(np.sqrt(m))
+    iy, ix = np.meshgrid(np.arange(side), np.arange(side), indexing="ij")
+    st[:, 0], st[:, 1], st[:, 4] = 1.0 + ix.ravel() * 0.06, 1.0 + iy.ravel() * 0.06, 0.7
+    g.getStateBuffer().copy_(torch.from_numpy(st))
+    mask = np.zeros((256, 256, 4), np.float32)
+    mask[:8, :, 3] = mask[-8:, :, 3] = mask[:, :8, 3] = mask[:, -8:, 3] = 1
+    g.computeBorder(torch.from_numpy(mask).cuda(), stream)
+    for _ in range(3):
+        g.compute(stream)
+    assert g.sync_status() == 0
+    done()
+    print("profile suite ok", flush=True)
+
+
 def run_reference(args, rank, world):
     """--impl reference: the CPU port of the reference kernels on a bounded sample."""
     if rank != 0:
@@ -430,7 +535,14 @@ def main(argv=None) -> int:
     ap.add_argument("--quick", action="store_true", help="skip e2e/profile/baseline legs (for ncu)")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / sort / 2D side measurements")
     ap.add_argument("--brick-width", type=int, default=0, help="cells per neighbour brick (0: library default)")
+    ap.add_argument("--profile-suite", action="store_true",
+                    help="run every hot path once, untimed (the workload of the per-kernel ncu summary)")
     args = ap.parse_args(argv)
+    if args.profile_suite:
+        import torch
+        torch.cuda.set_device(0)
+        profile_suite(torch.cuda.current_stream())
+        return 0
     rank, world, local = env_rank()
     if args.impl == "reference":
         return run_reference(args, rank, world)
