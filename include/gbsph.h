@@ -474,7 +474,8 @@ GBSPH_API const char* gbsph_bvh_lines_last_error(gbsph_bvh_lines_t h);
  * sort is not differentiated); the count > 2, max(1, rho), velocity clamp and wall branches are
  * differentiated on the side the forward step took. Memory: a checkpoint (position, velocity,
  * force) every `checkpoint_every` steps; backward() recomputes one segment at a time from its
- * checkpoint, recording 56 bytes per particle per step of that segment.
+ * checkpoint, recording 316 bytes per particle per step of that segment (sorted state, force,
+ * permutation, keys and the density pass's neighbour list of up to 64 entries).
  * Requires keyMode GBSPH_KEY_LINEAR_GRID, dims 3 and no integrate hook.
  * ---------------------------------------------------------------------------------------- */
 typedef struct gbsph_adjoint3d_s* gbsph_adjoint3d_t;

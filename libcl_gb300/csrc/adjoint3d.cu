@@ -4,10 +4,12 @@
 // force) taken before every K-th step. backward(): for each segment of K steps, last first,
 // the fluid is reset to the segment's checkpoint and stepped again with force recording on;
 // after each step the permutation, sorted keys, sorted state and the force after the clip box
-// are copied into the segment's tape (one kernel). The step's adjoint then runs in reverse
-// over the tape: post (integration, clamp, walls; builds the step's cell table) -> force
-// (gather) -> density (gather). The recomputed steps are the same kernels on the same inputs,
-// so the tape holds exactly the forward's states.
+// are copied into the segment's tape (one kernel), and the density pass writes each
+// particle's neighbour list (sorted indices) into the step's tape slot. The step's adjoint
+// then runs in reverse over the tape: post (integration, clamp, walls; builds the step's cell
+// table) -> force (gather over the lists) -> density (gather over the lists); particles
+// without a list (overflow, unstaged brick) walk the cell table. The recomputed steps are the
+// same kernels on the same inputs, so the tape holds exactly the forward's states.
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -26,6 +28,10 @@ struct gbsph_adjoint3d_s {
     float4* ckpt = nullptr;  // nseg x {pos, vel, force} x n4
     float4* fin = nullptr;   // {pos, vel, force} x n4
     char* tape = nullptr;    // `every` slots
+    uint32_t* lists = nullptr;  // `every` slots of n4 x NBR_CAP recorded neighbours
+    uint32_t* lcnt = nullptr;   // `every` slots of n4 list lengths
+    uint32_t* slot_dev = nullptr;  // the slot the recording step writes
+    uint32_t* slot_ids = nullptr;  // 0, 1, ..., every - 1 (copied into slot_dev)
     float4 *w = nullptr, *gxs = nullptr, *gvs = nullptr, *gx = nullptr, *gv = nullptr, *rec = nullptr;
     float* gS = nullptr;
     double2* acc = nullptr;
@@ -51,6 +57,8 @@ size_t slot_bytes(size_t n4) { return n4 * (4 + 4 + 16 + 16 + 16); }
 StepTape slot(const A* a, uint32_t k) {
     char* p = a->tape + slot_bytes(a->n4) * k;
     StepTape t;
+    t.nbr = a->lists + (size_t)k * a->n4 * NBR_CAP;
+    t.cnt = a->lcnt + (size_t)k * a->n4;
     t.spos = (float4*)p;
     p += a->n4 * 16;
     t.svel = (float4*)p;
@@ -104,6 +112,10 @@ int backward_segment(A* a, const FluidAccess& fa, const KParams& kp, uint32_t se
     const uint32_t s0 = seg * a->every, s1 = std::min(a->steps, s0 + a->every);
     RC(copy_state(a, fa, a->ckpt + (size_t)seg * 3 * a->n4, true, s));
     for (uint32_t st = s0; st < s1; st++) {
+        const uint32_t k = st - s0;  // the tape slot this step's lists go to
+        GBSPH_CUDA_TRY(&a->last_error, cudaMemcpyAsync(a->slot_dev, a->slot_ids + k, 4, cudaMemcpyDeviceToDevice, s));
+        // no list unless the step's density pass records one (the per-stage kernels do not)
+        GBSPH_CUDA_TRY(&a->last_error, cudaMemsetAsync(a->lcnt + (size_t)k * a->n4, 0xFF, a->n4 * 4, s));
         const int rc = gbsph_fluid3d_compute(a->fluid, (void*)s);
         if (rc) return fail(&a->last_error, rc, std::string("recompute: ") + gbsph_fluid3d_last_error(a->fluid));
         k_tape_record<<<grid1(a->n), 256, 0, s>>>(slot(a, st - s0), fa.index, fa.keys, fa.spos, fa.svel, a->rec,
@@ -117,8 +129,8 @@ int backward_segment(A* a, const FluidAccess& fa, const KParams& kp, uint32_t se
         uint2* other = a->tables + (size_t)((st + 1) & 1) * a->table_cells;
         const uint32_t* keys_next = st + 1 < s1 ? slot(a, st + 1 - s0).keys : nullptr;
         k_adj_post<<<grid1(a->n), 256, 0, s>>>(t, a->gx, a->gv, a->w, a->gxs, a->gvs, own, other, keys_next, kp);
-        k_adj_force<<<grid1(a->n), 256, 0, s>>>(t, own, a->w, a->gxs, a->gvs, a->gS, a->acc, kp, c45);
-        k_adj_density<<<grid1(a->n), 256, 0, s>>>(t, own, a->gS, a->gxs, a->gvs, a->gx, a->gv, kp);
+        k_adj_force<<<grid1(a->n * ADJ_LANES), 256, 0, s>>>(t, own, a->w, a->gxs, a->gvs, a->gS, a->acc, kp, c45);
+        k_adj_density<<<grid1(a->n * ADJ_LANES), 256, 0, s>>>(t, own, a->gS, a->gxs, a->gvs, a->gx, a->gv, kp);
         GBSPH_CUDA_TRY(&a->last_error, cudaGetLastError());
     }
     return GBSPH_OK;
@@ -141,8 +153,9 @@ GBSPH_API int gbsph_adjoint3d_create(gbsph_adjoint3d_t* out, gbsph_fluid3d_t flu
     a->n = gbsph_fluid3d_get_particle_count(fluid);
     a->n4 = (a->n + 63) & ~size_t(63);
     const size_t n4 = a->n4;
+    const size_t list_words = (size_t)a->every * n4 * (NBR_CAP + 1);
     const size_t bytes = (size_t)a->nseg * 3 * n4 * 16 + 3 * n4 * 16 + a->every * slot_bytes(n4) +
-                         6 * n4 * 16 + n4 * 4 + n4 * 16;
+                         6 * n4 * 16 + n4 * 4 + n4 * 16 + list_words * 4 + ((size_t)a->every + 64) * 4;
     if (cudaGetDevice(&a->device) != cudaSuccess || cudaMalloc(&a->block, bytes) != cudaSuccess) {
         cudaGetLastError();
         delete a;
@@ -163,6 +176,21 @@ GBSPH_API int gbsph_adjoint3d_create(gbsph_adjoint3d_t* out, gbsph_fluid3d_t flu
     a->acc = (double2*)p;
     p += n4 * 16;
     a->gS = (float*)p;
+    p += n4 * 4;
+    a->lists = (uint32_t*)p;
+    p += (size_t)a->every * n4 * NBR_CAP * 4;
+    a->lcnt = (uint32_t*)p;
+    p += (size_t)a->every * n4 * 4;
+    a->slot_dev = (uint32_t*)p;
+    a->slot_ids = a->slot_dev + 64;
+    std::vector<uint32_t> ids(a->every);
+    for (uint32_t k = 0; k < a->every; k++) ids[k] = k;
+    if (cudaMemcpy(a->slot_ids, ids.data(), (size_t)a->every * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(a->block);
+        delete a;
+        return GBSPH_ERR_CUDA;
+    }
     *out = a;
     return GBSPH_OK;
 }
@@ -219,7 +247,7 @@ GBSPH_API int gbsph_adjoint3d_backward(gbsph_adjoint3d_t a, const float* grad_po
     const float c45 = (float)(45.0 / (pi * std::pow((double)a->params.cellSize, 6.0)));
     {
         RecordGuard guard{a->fluid};
-        fluid3d_set_record(a->fluid, a->rec);
+        fluid3d_set_record(a->fluid, a->rec, a->lists, a->lcnt, a->slot_dev, (uint32_t)a->n4);
         for (uint32_t seg = a->nseg; seg-- > 0;) RC(backward_segment(a, fa, kp, seg, c45, s));
     }
     RC(copy_state(a, fa, a->fin, true, s));

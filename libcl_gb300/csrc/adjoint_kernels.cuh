@@ -9,8 +9,9 @@
 //   v'_o  = v_o + clamp(F_i) dt,   x'_o = x_o + v'_o dt
 // with d_ij = x_i - x_j, r = |d_ij|, Cv = mu * 45 / (pi h^6). The neighbour relation is
 // symmetric, so the loss terms of a pair {i, j} depend only on w_i - w_j (w = m dL/dF) and
-// dL/dS_i + dL/dS_j: each kernel gathers over its own particle's neighbours and nothing is
-// scattered (deterministic, no atomics). The count > 2, max(1, .), clamp and wall branches are
+// dL/dS_i + dL/dS_j: each kernel gathers over its own particle's neighbours (the list the
+// forward's density pass recorded, or the cells) and nothing is scattered (deterministic, no
+// atomics). The count > 2, max(1, .), clamp and wall branches are
 // differentiated on the side the forward step took.
 #pragma once
 
@@ -29,6 +30,8 @@ struct StepTape {
     float4* spos;
     float4* svel;
     float4* fwall;
+    const uint32_t* nbr;  // the density pass's neighbour lists (NBR_CAP per particle, sorted indices)
+    const uint32_t* cnt;  // their lengths, or REC_SCAN: walk the cells instead
 };
 
 static __global__ void k_tape_record(StepTape dst, const uint32_t* __restrict__ index,
@@ -43,12 +46,24 @@ static __global__ void k_tape_record(StepTape dst, const uint32_t* __restrict__ 
     dst.fwall[i] = fwall[i];
 }
 
-// Calls f(j, dx, dy, dz, r2) for every neighbour j != i with sqrtf(r2) < h, walking the 27
-// neighbour cells of the LINEAR_GRID table in z, y, x order.
+// Lanes that share a particle in the gather kernels below: lane q takes entries q, q + 4, ...
+// of the particle's list (or candidates q, q + 4, ... of each neighbour cell), and the lanes'
+// partial sums are added with shuffles in a fixed order (deterministic).
+constexpr uint32_t ADJ_LANES = 4;
+
+__device__ __forceinline__ float adj_lane_sum(float v) {
+#pragma unroll
+    for (uint32_t m = ADJ_LANES >> 1; m > 0; m >>= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    return v;
+}
+
+// Calls f(j, dx, dy, dz, r2) for every neighbour j != i with sqrtf(r2) < h among candidates
+// q, q + ADJ_LANES, ... of each of the 27 neighbour cells of the LINEAR_GRID table (z, y, x
+// order).
 template <class F>
 __device__ __forceinline__ void for_each_neighbour(const KParams& kp, const uint2* __restrict__ table,
                                                    const float4* __restrict__ spos, uint32_t i, const float4& pi,
-                                                   F&& f) {
+                                                   uint32_t q, F&& f) {
     int gx, gy, gz;
     grid_position(kp, pi, gx, gy, gz);
     gx = clampi(gx, 0, kp.nx - 1);
@@ -66,7 +81,7 @@ __device__ __forceinline__ void for_each_neighbour(const KParams& kp, const uint
                 if (cx < 0 || cx >= kp.nx) continue;
                 const uint2 e = table[row + (uint32_t)cx];
                 if (e.x == EMPTY) continue;
-                for (uint32_t j = e.x; j < e.y; j++) {
+                for (uint32_t j = e.x + q; j < e.y; j += ADJ_LANES) {
                     if (j == i) continue;
                     const float4 pj = spos[j];
                     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -75,6 +90,28 @@ __device__ __forceinline__ void for_each_neighbour(const KParams& kp, const uint
                 }
             }
         }
+    }
+}
+
+// Calls f(j, dx, dy, dz, r2) for lane q's share of the neighbours j != i of the recorded step:
+// entries q, q + ADJ_LANES, ... of the list the density pass recorded for i, or (list
+// overflowed, brick not staged) lane q's candidates of the cell walk.
+template <class F>
+__device__ __forceinline__ void for_each_recorded(const KParams& kp, const StepTape& t, const uint2* __restrict__ table,
+                                                  uint32_t i, const float4& pi, uint32_t q, F&& f) {
+    const uint32_t n = t.cnt[i];
+    if (n == REC_SCAN) {
+        for_each_neighbour(kp, table, t.spos, i, pi, q, f);
+        return;
+    }
+    const uint32_t* l = t.nbr + (size_t)i * NBR_CAP;
+    for (uint32_t e = q; e < n; e += ADJ_LANES) {
+        const uint32_t j = l[e];
+        if (j == i) continue;
+        const float4 pj = t.spos[j];
+        const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        if (r2 < kp.r2_thresh) f(j, dx, dy, dz, r2);
     }
 }
 
@@ -134,20 +171,23 @@ static __global__ void __launch_bounds__(256) k_adj_post(StepTape t, const float
 // dL/dx and dL/dv, writes dL/dS (zero where the forward clamped the density to 1 or set it to
 // rho0 because count <= 2), and accumulates per particle (particle order, FP64) the stiffness
 // term (rho - rho0) dL/dp and the viscosity term dL/dmu = (45 / (pi h^6)) w . B.
+// ADJ_LANES threads per particle.
 static __global__ void __launch_bounds__(256) k_adj_force(StepTape t, const uint2* __restrict__ table,
                                                           const float4* __restrict__ w, float4* __restrict__ gxs,
                                                           float4* __restrict__ gvs, float* __restrict__ gS,
                                                           double2* __restrict__ acc, KParams kp, float c45) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp.n) return;
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gt / ADJ_LANES, q = gt % ADJ_LANES;
+    const bool live = i < kp.n;
     const float4* __restrict__ spos = t.spos;
     const float4* __restrict__ svel = t.svel;
-    const float4 xi = spos[i], vi = svel[i], wi = w[i];
+    const float4 xi = live ? spos[i] : make_float4(0.f, 0.f, 0.f, 1.f), vi = live ? svel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wi = live ? w[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float rho_i = xi.w, p_i = vi.w, h = kp.h, cp = kp.cpress, cv = kp.cvisc;
     float3 ax = make_float3(0.f, 0.f, 0.f), av = make_float3(0.f, 0.f, 0.f), bsum = make_float3(0.f, 0.f, 0.f);
     float ap = 0.f, arho = 0.f;
     int count = 0;
-    for_each_neighbour(kp, table, spos, i, xi, [&](uint32_t j, float dx, float dy, float dz, float r2) {
+    if (live) for_each_recorded(kp, t, table, i, xi, q, [&](uint32_t j, float dx, float dy, float dz, float r2) {
         count++;
         if (!(r2 > 0.0f)) return;  // coincident particles exert no force
         const float4 xj = spos[j], vj = svel[j], wj = w[j];
@@ -174,6 +214,13 @@ static __global__ void __launch_bounds__(256) k_adj_force(StepTape t, const uint
         bsum.y += dvy * dh;
         bsum.z += dvz * dh;
     });
+    ax = make_float3(adj_lane_sum(ax.x), adj_lane_sum(ax.y), adj_lane_sum(ax.z));
+    av = make_float3(adj_lane_sum(av.x), adj_lane_sum(av.y), adj_lane_sum(av.z));
+    bsum = make_float3(adj_lane_sum(bsum.x), adj_lane_sum(bsum.y), adj_lane_sum(bsum.z));
+    ap = adj_lane_sum(ap);
+    arho = adj_lane_sum(arho);
+    count = (int)adj_lane_sum((float)count);
+    if (!live || q != 0) return;
     float4 g = gxs[i];
     gxs[i] = make_float4(g.x + ax.x, g.y + ax.y, g.z + ax.z, 0.f);
     g = gvs[i];
@@ -189,23 +236,27 @@ static __global__ void __launch_bounds__(256) k_adj_force(StepTape t, const uint
 
 // Density sum, backwards: dL/dx_i += -6 sum_j (h^2 - r^2)^2 d_ij (dL/dS_i + dL/dS_j); the
 // step's input gradients go back to particle order.
+// ADJ_LANES threads per particle.
 static __global__ void __launch_bounds__(256) k_adj_density(StepTape t, const uint2* __restrict__ table,
                                                             const float* __restrict__ gS,
                                                             const float4* __restrict__ gxs,
                                                             const float4* __restrict__ gvs, float4* __restrict__ gx,
                                                             float4* __restrict__ gv, KParams kp) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp.n) return;
-    const float4 xi = t.spos[i];
-    const float gSi = gS[i];
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = gt / ADJ_LANES, q = gt % ADJ_LANES;
+    const bool live = i < kp.n;
+    const float4 xi = live ? t.spos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float gSi = live ? gS[i] : 0.f;
     float3 a = make_float3(0.f, 0.f, 0.f);
-    for_each_neighbour(kp, table, t.spos, i, xi, [&](uint32_t j, float dx, float dy, float dz, float r2) {
+    if (live) for_each_recorded(kp, t, table, i, xi, q, [&](uint32_t j, float dx, float dy, float dz, float r2) {
         const float tt = kp.h2 - r2;
         const float c = -6.0f * tt * tt * (gSi + gS[j]);
         a.x = fmaf(c, dx, a.x);
         a.y = fmaf(c, dy, a.y);
         a.z = fmaf(c, dz, a.z);
     });
+    a = make_float3(adj_lane_sum(a.x), adj_lane_sum(a.y), adj_lane_sum(a.z));
+    if (!live || q != 0) return;
     const uint32_t o = t.index[i];
     const float4 g = gxs[i];
     gx[o] = make_float4(g.x + a.x, g.y + a.y, g.z + a.z, 0.f);

@@ -73,6 +73,10 @@ struct gbsph_fluid3d_s {
     size_t scratch_bytes = 0;
     uint32_t* err = nullptr;
     float4* rec_force = nullptr;  // set by an adjoint while it records a step
+    uint32_t* rec_nbr = nullptr;
+    uint32_t* rec_cnt = nullptr;
+    const uint32_t* rec_slot = nullptr;
+    uint32_t rec_n4 = 0;
     gbsph_fluid3d_hook_fn hook = nullptr;
     void* hook_user = nullptr;
     int opt_fused = 1, opt_graph = 1, opt_bw = 16, opt_profile = 0;
@@ -180,6 +184,10 @@ KParams make_kparams(const H* h) {
     k.bxn = k.nx > 0 ? (k.nx + k.bw - 1) / k.bw : 0;
     k.n = (uint32_t)h->n;
     k.rec_force = h->rec_force;
+    k.rec_nbr = h->rec_nbr;
+    k.rec_cnt = h->rec_cnt;
+    k.rec_slot = h->rec_slot;
+    k.rec_n4 = h->rec_n4;
     return k;
 }
 
@@ -506,7 +514,14 @@ int fluid3d_access(gbsph_fluid3d_t h, FluidAccess* a, KParams* kp) {
     return GBSPH_OK;
 }
 
-void fluid3d_set_record(gbsph_fluid3d_t h, float4* rec) { h->rec_force = rec; }
+void fluid3d_set_record(gbsph_fluid3d_t h, float4* rec, uint32_t* rec_nbr, uint32_t* rec_cnt, const uint32_t* rec_slot,
+                        uint32_t rec_n4) {
+    h->rec_force = rec;
+    h->rec_nbr = rec_nbr;
+    h->rec_cnt = rec_cnt;
+    h->rec_slot = rec_slot;
+    h->rec_n4 = rec_n4;
+}
 
 }  // namespace gbsph
 

@@ -51,6 +51,14 @@ struct KParams {
     const SceneDev* scenes;  // batches only: n_scenes entries, sorted by part/cell/brick offsets
     int n_scenes;
     float4* rec_force;  // when set: receives each particle's force after the clip box, before the clamp
+    // When set (brick kernels): slot *rec_slot of rec_nbr (rec_n4 * NBR_CAP words per slot)
+    // receives each particle's in-range neighbours (itself included) as sorted indices,
+    // NBR_CAP per particle, and slot *rec_slot of rec_cnt (rec_n4 words) their number, or
+    // REC_SCAN where the list overflowed or the brick was not staged.
+    uint32_t* rec_nbr;
+    uint32_t* rec_cnt;
+    const uint32_t* rec_slot;
+    uint32_t rec_n4;
 };
 
 // Index of the scene whose range [off, next off) holds v (binary search over `n` scenes).
@@ -640,6 +648,7 @@ constexpr uint32_t LIST_STAGE_MAX = 160;        // targets per brick whose lists
 constexpr uint32_t GROUP_MAX = 16;              // targets a warp takes at once (both passes)
 constexpr uint32_t NBR_SUBLISTS = 8;            // at most 8 lanes (sub-lists) per target
 constexpr uint64_t NBR_SCAN = 1ull << 63;       // nbr_meta: the force pass scans for this target
+constexpr uint32_t REC_SCAN = 0xFFFFFFFFu;      // rec_cnt: no recorded list for this particle
 
 
 // Dynamic shared memory of the brick kernels.
@@ -799,6 +808,31 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                     }
                 }
                 const bool ovf = !staged || nk >= sub;
+                if (kp.rec_nbr) {
+                    // recording (an adjoint's recomputation): the target's sub-lists, concatenated
+                    // in q order, as sorted indices; lane q writes its own entries after those
+                    // of the lanes q' < q of its target
+                    uint32_t before = active ? nk : 0u;
+#pragma unroll
+                    for (uint32_t st = 1; st < NBR_SUBLISTS; st <<= 1) {
+                        const uint32_t v = __shfl_up_sync(0xffffffffu, before, (st * tg) & 31u);
+                        if (q >= st && st < Q) before += v;
+                    }
+                    before -= active ? nk : 0u;  // exclusive
+                    const uint32_t anyovf = __ballot_sync(0xffffffffu, active && ovf) & (L.group[tg] << ti);
+                    if (active && !anyovf) {
+                        const size_t slot = *kp.rec_slot;
+                        uint32_t* out = kp.rec_nbr + (slot * kp.rec_n4 + gi) * NBR_CAP + before;
+                        for (uint32_t e = 0; e < nk; ++e) {
+                            const uint32_t sidx = my[e];
+                            uint32_t g = sidx;
+#pragma unroll
+                            for (int r = 0; r < R; ++r)
+                                if (sidx >= S.base[r]) g = sidx - S.base[r] + S.lo[r];
+                            out[e] = g;
+                        }
+                    }
+                }
                 acc = reduce_q(acc, q, Q, tg);
                 const float cnt = reduce_q((float)nk, q, Q, tg);
                 const uint32_t om = __ballot_sync(0xffffffffu, active && ovf) & (L.group[tg] << ti);
@@ -817,6 +851,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                     reinterpret_cast<float*>(svel)[4 * (size_t)gi + 3] = p;
                     const uint64_t lens = *reinterpret_cast<const uint64_t*>(wcnt[warp][ti]);
                     nbr_meta[gi] = om ? NBR_SCAN : (Q < 8 ? lens & ((1ull << (8 * Q)) - 1ull) : lens);
+                    if (kp.rec_cnt) kp.rec_cnt[(size_t)*kp.rec_slot * kp.rec_n4 + gi] = om ? REC_SCAN : (uint32_t)(cnt + 0.5f);
                 }
                 // copy the group's lists out. A brick's lists fill the brick's targets' rows of
                 // nbr, stored chunk-major: the 16-byte chunk ch (entries 8ch..8ch+7) of the
