@@ -117,80 +117,139 @@ __device__ __forceinline__ void cells_of(const K2& k, float px, float py, int& x
     y1 = min(gy + 1, k.ncy - 1);
 }
 
-// clComputePressure (libCL/phys/oclFluid2D.cl:185-245).
+// The neighbour loops of clComputePressure / clComputePosition visit cells x = x0..x1 (outer),
+// y = y0..y1 (inner) and the particles of each cell in sorted order, summing in that order.
+// Here a warp takes one particle: the candidates (the cells' ranges, concatenated in the
+// reference's order) are dealt to the lanes 32 at a time, each lane computes its candidate's
+// terms, and the sums take the in-range terms one by one in candidate order (broadcast by
+// shuffles), so every operation and its order are the reference's.
+struct Cand2 {
+    uint32_t pre;    // lane c < 9: candidates before cell c (of the concatenation)
+    uint32_t start;  // lane c < 9: the cell's first sorted index
+    uint32_t total;  // candidates of all cells (every lane)
+};
+
+__device__ __forceinline__ Cand2 cand2_setup(const K2& k, float px, float py, const uint32_t* __restrict__ cs,
+                                             const uint32_t* __restrict__ ce) {
+    const uint32_t lane = threadIdx.x & 31u;
+    int x0, x1, y0, y1;
+    cells_of(k, px, py, x0, x1, y0, y1);
+    const int ny = y1 - y0 + 1, nc = (x1 - x0 + 1) * ny;
+    uint32_t len = 0, st = 0;
+    if ((int)lane < nc) {
+        const int c = (y0 + (int)lane % ny) * k.ncx + x0 + (int)lane / ny;  // x outer, y inner
+        st = cs[c];
+        if (st != EMPTY2) len = ce[c] - st;
+    }
+    uint32_t incl = len;
+#pragma unroll
+    for (int o = 1; o < 16; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += v;
+    }
+    Cand2 c;
+    c.pre = incl - len;
+    c.start = st;
+    c.total = __shfl_sync(0xffffffffu, incl, 8);
+    return c;
+}
+
+// Sorted index of candidate k < total (from the per-cell values held by lanes 0..8).
+__device__ __forceinline__ uint32_t cand2_index(const Cand2& c, uint32_t k) {
+    uint32_t j = 0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const uint32_t pre = __shfl_sync(0xffffffffu, c.pre, q), st = __shfl_sync(0xffffffffu, c.start, q);
+        if (k >= pre) j = st + (k - pre);
+    }
+    return j;
+}
+
+// clComputePressure (libCL/phys/oclFluid2D.cl:185-245), a warp per particle.
 __global__ void k2_pressure(const P2* __restrict__ srt, float4* __restrict__ ps, const uint32_t* __restrict__ cs,
                             const uint32_t* __restrict__ ce, const float4* __restrict__ bstate, K2 k) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (i >= k.n) return;  // whole warps
     const P2 pi = srt[i];
-    int x0, x1, y0, y1;
-    cells_of(k, pi.px, pi.py, x0, x1, y0, y1);
     float density = 0.f, nearDensity = 0.f;
     const float4 wall = sample(bstate, k.W, k.H, fd(pi.px, k.cW), fd(pi.py, k.cH));
     if (wall.x != 0.f) {
         density = fa(density, wall.x);
         nearDensity = fa(nearDensity, wall.y);
     }
-    for (int x = x0; x <= x1; x++)
-        for (int y = y0; y <= y1; y++) {
-            const int c = y * k.ncx + x;
-            const uint32_t start = cs[c];
-            if (start == EMPTY2) continue;
-            const uint32_t end = ce[c];
-            for (uint32_t j = start; j < end; j++) {
-                if (j == i) continue;
-                const float dx = fs(srt[j].px, pi.px), dy = fs(srt[j].py, pi.py);
-                const float r = len2(dx, dy);
-                if (r > 0.0000001f && r < k.h) {
-                    const float a = fs(1.f, fd(r, k.h));
-                    density = fa(density, fm(fm(fm(fm(k.m, a), a), a), k.kNorm));
-                    nearDensity = fa(nearDensity, fm(fm(fm(fm(fm(k.m, a), a), a), a), k.kNearNorm));
-                }
+    const Cand2 c = cand2_setup(k, pi.px, pi.py, cs, ce);
+    for (uint32_t base = 0; base < c.total; base += 32) {
+        const uint32_t kk = base + lane;
+        const uint32_t j = cand2_index(c, kk);
+        bool in = false;
+        float td = 0.f, tn = 0.f;
+        if (kk < c.total && j != i) {
+            const float dx = fs(srt[j].px, pi.px), dy = fs(srt[j].py, pi.py);
+            const float r = len2(dx, dy);
+            if (r > 0.0000001f && r < k.h) {
+                const float a = fs(1.f, fd(r, k.h));
+                td = fm(fm(fm(fm(k.m, a), a), a), k.kNorm);
+                tn = fm(fm(fm(fm(fm(k.m, a), a), a), a), k.kNearNorm);
+                in = true;
             }
         }
-    ps[i] = make_float4(density, nearDensity, fm(kStiffness, fs(density, fm(k.m, kRestDensity))),
-                        fm(kNearStiffness, nearDensity));
+        for (uint32_t m = __ballot_sync(0xffffffffu, in); m; m &= m - 1) {
+            const int b = __ffs(m) - 1;
+            density = fa(density, __shfl_sync(0xffffffffu, td, b));
+            nearDensity = fa(nearDensity, __shfl_sync(0xffffffffu, tn, b));
+        }
+    }
+    if (lane == 0)
+        ps[i] = make_float4(density, nearDensity, fm(kStiffness, fs(density, fm(k.m, kRestDensity))),
+                            fm(kNearStiffness, nearDensity));
 }
 
-// clComputePosition (libCL/phys/oclFluid2D.cl:247-326). The reference's viscosity term uses
-// vel_j - vel_j (:299), which is zero, so it never contributes and is not evaluated here.
+// clComputePosition (libCL/phys/oclFluid2D.cl:247-326), a warp per particle. The reference's
+// viscosity term uses vel_j - vel_j (:299), which is zero, so it never contributes and is not
+// evaluated here.
 __global__ void k2_position(const P2* __restrict__ srt, const float4* __restrict__ ps, float2* __restrict__ relaxed,
                             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                             const float4* __restrict__ bstate, const float4* __restrict__ bvec, K2 k) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k.n) return;
+    const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (i >= k.n) return;  // whole warps
     const float4 si = ps[i];
     const P2 pi = srt[i];
-    int x0, x1, y0, y1;
-    cells_of(k, pi.px, pi.py, x0, x1, y0, y1);
     float rx = pi.px, ry = pi.py;
     const float dt2 = fm(k.dT, k.dT);
-    for (int x = x0; x <= x1; x++)
-        for (int y = y0; y <= y1; y++) {
-            const int c = y * k.ncx + x;
-            const uint32_t start = cs[c];
-            if (start == EMPTY2) continue;
-            const uint32_t end = ce[c];
-            for (uint32_t j = start; j < end; j++) {
-                if (j == i) continue;
-                const float dx = fs(srt[j].px, pi.px), dy = fs(srt[j].py, pi.py);
-                const float r = len2(dx, dy);
-                if (r > 0.0000001f && r < k.h) {
-                    const float4 sj = ps[j];
-                    const float a = fs(1.f, fd(r, k.h));
-                    const float near = fm(fm(fm(fm(fa(si.w, sj.w), a), a), a), k.kNearNorm);
-                    const float far = fm(fm(fm(fa(si.z, sj.z), a), a), k.kNorm);
-                    const float d = fd(fm(dt2, fa(near, far)), 2.f);
-                    const float rm = fm(r, k.m);
-                    rx = fs(rx, fd(fm(dx, d), rm));
-                    ry = fs(ry, fd(fm(dy, d), rm));
-                    const float surf = fd(fm(fm(fm(dt2, fd(kSurfaceTension, k.m)), k.m),
-                                             fa(fm(fm(fm(a, a), a), k.kNearNorm), fm(fm(a, a), k.kNorm))), 2.f);
-                    rx = fa(rx, fm(surf, dx));
-                    ry = fa(ry, fm(surf, dy));
-                }
+    const Cand2 c = cand2_setup(k, pi.px, pi.py, cs, ce);
+    for (uint32_t base = 0; base < c.total; base += 32) {
+        const uint32_t kk = base + lane;
+        const uint32_t j = cand2_index(c, kk);
+        bool in = false;
+        float ux = 0.f, uy = 0.f, wx = 0.f, wy = 0.f;
+        if (kk < c.total && j != i) {
+            const float dx = fs(srt[j].px, pi.px), dy = fs(srt[j].py, pi.py);
+            const float r = len2(dx, dy);
+            if (r > 0.0000001f && r < k.h) {
+                const float4 sj = ps[j];
+                const float a = fs(1.f, fd(r, k.h));
+                const float near = fm(fm(fm(fm(fa(si.w, sj.w), a), a), a), k.kNearNorm);
+                const float far = fm(fm(fm(fa(si.z, sj.z), a), a), k.kNorm);
+                const float d = fd(fm(dt2, fa(near, far)), 2.f);
+                const float rm = fm(r, k.m);
+                ux = fd(fm(dx, d), rm);
+                uy = fd(fm(dy, d), rm);
+                const float surf = fd(fm(fm(fm(dt2, fd(kSurfaceTension, k.m)), k.m),
+                                         fa(fm(fm(fm(a, a), a), k.kNearNorm), fm(fm(a, a), k.kNorm))), 2.f);
+                wx = fm(surf, dx);
+                wy = fm(surf, dy);
+                in = true;
             }
         }
+        for (uint32_t m = __ballot_sync(0xffffffffu, in); m; m &= m - 1) {
+            const int b = __ffs(m) - 1;
+            rx = fs(rx, __shfl_sync(0xffffffffu, ux, b));
+            ry = fs(ry, __shfl_sync(0xffffffffu, uy, b));
+            rx = fa(rx, __shfl_sync(0xffffffffu, wx, b));
+            ry = fa(ry, __shfl_sync(0xffffffffu, wy, b));
+        }
+    }
+    if (lane != 0) return;
     const float4 wall = sample(bstate, k.W, k.H, fd(rx, k.cW), fd(ry, k.cH));
     if (wall.x != 0.f) {
         const float4 normal = sample(bvec, k.W, k.H, fd(rx, k.cW), fd(ry, k.cH));
@@ -478,8 +537,9 @@ int enqueue2(H2* h, const K2& k, cudaStream_t s) {
     k2_reorder<<<grid1(k.n), 256, 0, s>>>(h->index, (const P2*)h->state, h->sorted, k.n);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     GBSPH_CUDA_TRY(&h->last_error, cell_bounds_launch(h->keys_c, k.n, h->cs, h->ce, h->table, h->err, s));
-    k2_pressure<<<grid1(k.n), 256, 0, s>>>(h->sorted, h->pstate, h->cs, h->ce, h->bstate, k);
-    k2_position<<<grid1(k.n), 256, 0, s>>>(h->sorted, h->pstate, h->relaxed, h->cs, h->ce, h->bstate, h->bvec, k);
+    const unsigned wgrid = (unsigned)(((size_t)k.n * 32 + 255) / 256);  // a warp per particle
+    k2_pressure<<<wgrid, 256, 0, s>>>(h->sorted, h->pstate, h->cs, h->ce, h->bstate, k);
+    k2_position<<<wgrid, 256, 0, s>>>(h->sorted, h->pstate, h->relaxed, h->cs, h->ce, h->bstate, h->bvec, k);
     k2_update<<<grid1(k.n), 256, 0, s>>>((P2*)h->state, h->prev, h->relaxed, h->index, k);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
