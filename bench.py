@@ -250,6 +250,23 @@ def extra_sort(stream) -> dict:
     ms = _time_steps(lambda: sorter.cell_bounds(k, cs, ce, stream), 5, stream) / 5
     out["cell_bounds_2^22_ms"] = ms
     assert sorter.sync_status() == 0
+    # CPU beside it: the restated reference sort (4-bit passes of 256-key blocks, host cores)
+    # at its largest accepted size, 4,190,208 pairs (it refuses 2^22), and std::stable_sort on
+    # the 16M uniform pairs
+    import oracle
+    ku = (SplitMix64(3).next_u64(n) >> np.uint64(32)).astype(np.uint32)
+    m = (1 << 22) - 4096
+    kk, vv = ku[:m].copy(), np.arange(m, dtype=np.uint32)
+    t0 = time.perf_counter()
+    assert oracle.radix_sort_reference(kk, vv, 0, 32) == 0
+    t_ref = time.perf_counter() - t0
+    kk, vv = ku.copy(), np.arange(n, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.stable_sort(kk, vv, 0, 32)
+    t_std = time.perf_counter() - t0
+    out["cpu"] = {"cores": oracle.num_threads(),
+                  "reference_sort_4190208_pairs_per_s": m / t_ref,
+                  "std_stable_sort_16m_pairs_per_s": n / t_std}
     return out
 
 
@@ -331,6 +348,20 @@ def extra_adjoint(stream) -> dict:
                      "forward_ms": t_fwd, "adjoint_forward_ms": t_a, "adjoint_backward_ms": t_b,
                      "fwd_plus_adj_over_fwd": (t_a + t_b) / t_fwd,
                      "fwd_plus_adj_particle_steps_per_s": sc.n * steps / ((t_a + t_b) * 1e-3)}
+        if name == "differentiable_block_64k":
+            # CPU beside it: the FP64 oracle's forward + adjoint on a 10-step sample (K = 5)
+            import oracle
+            p64 = sc.pos.astype(np.float64)
+            v64 = np.zeros_like(p64)
+            f64 = np.zeros_like(p64)
+            f64[:, :3] = np.array(list(sc.params.gravity)[:3])
+            g64 = np.zeros_like(p64)
+            g64[:, :3] = 1e-6
+            t0 = time.perf_counter()
+            oracle.adjoint_f64(p64, v64, f64, sc.params, 10, 5, g64)
+            dt = time.perf_counter() - t0
+            out[name]["cpu_fp64_fwd_plus_adj"] = {"cores": oracle.num_threads(), "sample_steps": 10,
+                                                  "particle_steps_per_s": sc.n * 10 / dt}
         del adj, f
         torch.cuda.empty_cache()
     return out
