@@ -48,6 +48,19 @@ enum {
 /* Human-readable name of a status code (static storage). */
 GBSPH_API const char* gbsph_status_string(int status);
 
+/* Failure-detection self-test (no counterpart in the reference). Runs, on the current device,
+ * a wait that nothing will complete and reports what the bound made of it:
+ *   which = 0: a one-sweep sort pass whose first tile never runs (its tile counter starts at
+ *              1), so the next tile's decoupled look-back waits on a status word nobody
+ *              writes;
+ *   which = 1: a kernel that waits on a shared-memory mbarrier expecting bytes that no copy
+ *              delivers.
+ * Each wait gives up after about one second, sets its device error bit and the kernel ends;
+ * the call synchronises `stream` and returns GBSPH_ERR_DEVICE_TIMEOUT if that happened (and
+ * the context stays usable), GBSPH_OK if the wait somehow completed, or an argument/CUDA
+ * error. */
+GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream);
+
 /* ABI version: major*10000 + minor*100 + patch. */
 GBSPH_API int gbsph_version(void);
 

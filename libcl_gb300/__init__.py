@@ -140,6 +140,7 @@ SIGNATURES = {
     "gbsph_bvh_sync_status": (_I, [_P, _P]),
     "gbsph_bvh_last_error": (C.c_char_p, [_P]),
     "gbsph_bvh_collide": (_I, [_P, C.POINTER(Fluid3DParams), _P, _P, _P, _SZ, _P, _SZ, _P, _P]),
+    "gbsph_selftest_bounded_wait": (_I, [_I, _P]),
     "gbsph_bvh_lines_create": (_I, [C.POINTER(_P)]),
     "gbsph_bvh_lines_destroy": (_I, [_P]),
     "gbsph_bvh_lines_compute": (_I, [_P, _P, _SZ, _P]),

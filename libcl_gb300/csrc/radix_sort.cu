@@ -269,7 +269,44 @@ cudaError_t launch_pass(int ngather, const uint32_t* kin, const uint32_t* vin, u
     return launch_pass_items<IOTA, 16>(ngather, kin, vin, kout, vout, n, shift, bits, pass, scratch, err, g, s);
 }
 
+// A wait on an mbarrier that expects 16 bytes no copy will deliver: the bounded wait gives up
+// and sets DEV_ERR_MBAR_TIMEOUT (failure-detection self-test).
+__global__ void k_selftest_mbar(uint32_t* err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, 16u);
+        if (!mbar_wait_bounded(&bar, 0)) atomicOr(err, DEV_ERR_MBAR_TIMEOUT);
+    }
+}
+
 }  // namespace
+
+int selftest_mbarrier_timeout(cudaStream_t s) {
+    uint32_t* err = nullptr;
+    if (cudaMalloc(&err, 4) != cudaSuccess) {
+        cudaGetLastError();
+        return GBSPH_ERR_OUT_OF_MEMORY;
+    }
+    int rc = GBSPH_OK;
+    uint32_t bits = 0;
+    if (cudaMemsetAsync(err, 0, 4, s) != cudaSuccess) {
+        rc = GBSPH_ERR_CUDA;
+    } else {
+        k_selftest_mbar<<<1, 32, 0, s>>>(err);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess ||
+            cudaMemcpy(&bits, err, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = GBSPH_ERR_CUDA;
+        else
+            rc = (bits & DEV_ERR_MBAR_TIMEOUT) ? GBSPH_ERR_DEVICE_TIMEOUT : GBSPH_OK;
+    }
+    cudaFree(err);
+    return rc;
+}
 
 size_t onesweep_scratch_bytes(uint32_t n, int passes) {
     return SORT_HEADER_BYTES + (size_t)std::max(passes, 1) * sort_tiles(std::max(n, 1u)) * SORT_RADIX * 4;
@@ -479,6 +516,48 @@ GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream) {
                     "device error word 0x" + std::to_string(bits));
     }
     return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream) {
+    if (which != 0 && which != 1) return GBSPH_ERR_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (which == 1) return selftest_mbarrier_timeout(s);
+    // Two tiles of 2048 keys; the pass's tile counter starts at 1, so tile 0 never runs, the
+    // CTA that draws tile 1 looks back at tile 0's unwritten status until its bound expires,
+    // and the CTA that draws tile 2 finds no tile (a capacity error). The outputs stay inside
+    // the buffers: with an all-zero histogram every destination is a tile-local position.
+    constexpr int ITEMS = 8;
+    const uint32_t n = 2 * SORT_THREADS * ITEMS, tiles = 2;
+    const size_t scratch_bytes = SORT_HEADER_BYTES + (size_t)tiles * SORT_RADIX * 4;
+    char* block = nullptr;
+    const size_t bytes = scratch_bytes + 4 * (size_t)n * 4 + 256;
+    if (cudaMalloc(&block, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return GBSPH_ERR_OUT_OF_MEMORY;
+    }
+    int rc = GBSPH_OK;
+    uint32_t* scratch = (uint32_t*)block;
+    uint32_t* keys = (uint32_t*)(block + scratch_bytes);
+    uint32_t* kout = keys + n;
+    uint32_t* vout = kout + n;
+    uint32_t* err = vout + n;
+    const uint32_t one = 1;
+    SortGather g{};
+    if (cudaMemsetAsync(block, 0, bytes, s) != cudaSuccess ||
+        cudaMemcpyAsync(scratch + 4096 / 4, &one, 4, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+        rc = GBSPH_ERR_CUDA;
+    } else {
+        k_onesweep<true, 0, ITEMS><<<tiles, SORT_THREADS, 0, s>>>(keys, nullptr, kout, vout, n, 0, 8, 0, tiles, scratch,
+                                                                  err, g);
+        uint32_t bits = 0;
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess ||
+            cudaMemcpy(&bits, err, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = GBSPH_ERR_CUDA;
+        else
+            rc = (bits & DEV_ERR_LOOKBACK_TIMEOUT) ? GBSPH_ERR_DEVICE_TIMEOUT : GBSPH_OK;
+    }
+    cudaFree(block);
+    return rc;
 }
 
 GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h) {
