@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "fluid3d_access.h"
 
 using namespace gbsph;
@@ -415,8 +417,14 @@ int enqueue_staged(H* h, const KParams& kp, cudaStream_t s) {
     return GBSPH_OK;
 }
 
+// With GBSPH_OPT_PROFILE: an event between stages (gbsph_fluid3d_stage_times) and an NVTX
+// range per stage (named as the stage times; seen by nsys / ncu --nvtx, free otherwise).
 int mark(H* h, int i, cudaStream_t s) {
     if (!h->opt_profile) return GBSPH_OK;
+    static const char* const kStage[5] = {"gbsph front_end", "gbsph sort", "gbsph bounds", "gbsph density",
+                                          "gbsph forces"};
+    if (i > 0) nvtxRangePop();
+    if (i < 5) nvtxRangePushA(kStage[i]);
     if (!h->ev[i]) GBSPH_CUDA_TRY(&h->last_error, cudaEventCreate(&h->ev[i]));
     GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->ev[i], s));
     return GBSPH_OK;
