@@ -132,6 +132,55 @@ def gpu_ident(torch) -> str | None:
     return None
 
 
+def neighbour_flops(fluid, params, sample: int = 65536, seed: int = 9) -> dict:
+    """Algorithmic FP32 work of the neighbour passes on the fluid's current (sorted) state,
+    counted exactly on a random sample of particles: candidates of the 27-cell stencil and
+    in-range pairs (the particle itself included), then density = candidates x 9 + in-range
+    x 30 flops and forces = in-range x 60 flops per particle (the force pass evaluates only the
+    listed pairs)."""
+    import torch
+    nx, ny, nz = (int(g) for g in params.gridDim[:3])
+    cs, ce = fluid.cell_bounds(nx * ny * nz)
+    keys = fluid.getCellBuffer().long() & 0xFFFFFFFF
+    spos = fluid.getSortedPositionBuffer()[:, :3]
+    n = keys.numel()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    i = torch.randint(0, n, (min(sample, n),), device="cuda", generator=g)
+    k = keys[i]
+    x, y, z = k % nx, (k // nx) % ny, k // (nx * ny)
+    cs64 = cs.long() & 0xFFFFFFFF
+    ce64 = ce.long() & 0xFFFFFFFF
+    occ = torch.where(cs64 == 0xFFFFFFFF, torch.zeros_like(cs64), ce64 - cs64)
+    maxocc = int(occ.max().item())
+    thr = float(params.cellSize) ** 2
+    pi = spos[i]
+    cand = torch.zeros_like(k)
+    inr = torch.zeros_like(k)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                cx, cy, cz = x + dx, y + dy, z + dz
+                ok = (cx >= 0) & (cx < nx) & (cy >= 0) & (cy < ny) & (cz >= 0) & (cz < nz)
+                c = torch.where(ok, cx + nx * (cy + ny * cz), torch.zeros_like(cx))
+                st = cs64[c]
+                ln = torch.where(ok, occ[c], torch.zeros_like(c))
+                cand += ln
+                for m in range(maxocc):
+                    v = ln > m
+                    j = torch.where(v, st + m, torch.zeros_like(st))
+                    r2 = ((spos[j] - pi) ** 2).sum(dim=1)
+                    inr += (v & (r2 < thr)).long()
+    c_mean = float(cand.float().mean().item())
+    r_mean = float(inr.float().mean().item())
+    return {"sample_particles": int(i.numel()), "candidates_per_particle": c_mean,
+            "in_range_per_particle": r_mean, "density_flops_per_particle": 9 * c_mean + 30 * r_mean,
+            "forces_flops_per_particle": 60 * r_mean}
+
+
+def sm_count(torch) -> int:
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def load_scene(fluid, scene):
     import ctypes
     import torch
@@ -671,6 +720,15 @@ def main(argv=None) -> int:
         result["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
                               "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
                               "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": stage_ms[dom]}
+        fl = neighbour_flops(fluid, scene.params)
+        fp32_peak = sm_count(torch) * 128 * 2 * (result["clocks"].get("sm_mhz") or 2070.0) * 1e6 / 1e12
+        fl["fp32_peak_tflops"] = fp32_peak
+        fl["fp32_peak_source"] = "derived: SMs x 128 FP32 lanes x 2 (FMA) x median SM clock of the timed run"
+        for stg in ("density", "forces"):
+            tf = fl[f"{stg}_flops_per_particle"] * scene.n / (stage_ms[stg] * 1e-3) / 1e12
+            fl[f"{stg}_achieved_tflops"] = tf
+            fl[f"{stg}_fp32_frac"] = tf / fp32_peak
+        result["flops"] = fl
         step_bytes = sum(STAGE_BYTES_PER_PARTICLE.values()) * scene.n + 8 * n_cells_occ
         result["stages"] = {"ms": stage_ms, "gbs": stage_gbs, "occupied_cells": n_cells_occ,
                             "step_algorithmic_bytes": step_bytes,
