@@ -237,6 +237,16 @@ GBSPH_API int gbsph_fluid3d_set_integrate_hook(gbsph_fluid3d_t h, gbsph_fluid3d_
 GBSPH_API int gbsph_fluid3d_set_option(gbsph_fluid3d_t h, int option, int value);
 /* compute(oclDevice&) -- libCL/phys/oclFluid3D.cpp:293-342. Asynchronous on `stream`. */
 GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream);
+/* One step on state held in host memory, for callers that keep it there between steps (the
+ * reference's users map position/velocity/force to the host around compute(), e.g.
+ * libCL/TEST/main.cpp:222-236): the three float4[n] inputs are uploaded into the fluid's
+ * position/velocity/force buffers, the step runs, and the three buffers are downloaded into
+ * the outputs (which may be the inputs). With page-locked host memory the uploads of velocity
+ * and force overlap the hash, sort and density passes and the whole is one replayed graph;
+ * pageable memory works too, without the overlap. Asynchronous on `stream`. */
+GBSPH_API int gbsph_fluid3d_compute_host(gbsph_fluid3d_t h, const float* position_in, const float* velocity_in,
+                                         const float* force_in, float* position_out, float* velocity_out,
+                                         float* force_out, void* stream);
 /* One reference stage alone (GBSPH_STAGE_*), asynchronous on `stream`. */
 GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream);
 /* Copies the cell table out as two uint32 arrays of n_cells entries (device pointers),

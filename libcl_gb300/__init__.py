@@ -99,6 +99,7 @@ SIGNATURES = {
     "gbsph_fluid3d_set_integrate_hook": (_I, [_P, HOOK_FN, _P]),
     "gbsph_fluid3d_set_option": (_I, [_P, _I, _I]),
     "gbsph_fluid3d_compute": (_I, [_P, _P]),
+    "gbsph_fluid3d_compute_host": (_I, [_P, _P, _P, _P, _P, _P, _P, _P]),
     "gbsph_fluid3d_stage": (_I, [_P, _I, _P]),
     "gbsph_fluid3d_get_cell_bounds": (_I, [_P, _P, _P, _SZ, _P]),
     "gbsph_fluid3d_sync_status": (_I, [_P, _P]),
@@ -192,6 +193,15 @@ def _ptr(t) -> int:
     return 0 if t is None else int(t.data_ptr())
 
 
+def _host_ptr(a) -> int:
+    """Address of a contiguous float32 host tensor or numpy array."""
+    if hasattr(a, "data_ptr"):
+        assert not a.is_cuda and a.is_contiguous() and a.element_size() == 4, "a contiguous float32 CPU tensor"
+        return a.data_ptr()
+    assert a.flags["C_CONTIGUOUS"] and a.dtype.itemsize == 4, "a contiguous float32 array"
+    return a.ctypes.data
+
+
 def _stream(stream) -> int:
     if stream is None:
         import torch
@@ -282,6 +292,17 @@ class Fluid3D:
 
     def compute_raw(self, stream=None) -> int:
         return self._lib.gbsph_fluid3d_compute(self._h, _stream(stream))
+
+    def compute_host(self, position, velocity, force, position_out=None, velocity_out=None, force_out=None,
+                     stream=None) -> None:
+        """One step on host-resident state (gbsph_fluid3d_compute_host): CPU float32 tensors or
+        arrays [N, 4] (page-locked tensors give the overlapped path); the outputs default to
+        the inputs. Asynchronous on `stream`: synchronise before reading the outputs."""
+        outs = [position if position_out is None else position_out, velocity if velocity_out is None else velocity_out,
+                force if force_out is None else force_out]
+        self._check(self._lib.gbsph_fluid3d_compute_host(self._h, _host_ptr(position), _host_ptr(velocity),
+                                                         _host_ptr(force), *(_host_ptr(o) for o in outs),
+                                                         _stream(stream)))
 
     def stage(self, stage: int, stream=None) -> None:
         self._check(self._lib.gbsph_fluid3d_stage(self._h, stage, _stream(stream)))

@@ -88,6 +88,11 @@ struct gbsph_fluid3d_s {
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
     std::vector<char> gkey;
+    // compute_host: the step with its host copies, captured separately
+    cudaStream_t io_stream = nullptr;
+    cudaEvent_t io_ev[3] = {};  // fork, velocity uploaded, force uploaded
+    cudaGraphExec_t gexec_io = nullptr;
+    std::vector<char> gkey_io;
     std::string last_error;
 };
 
@@ -197,7 +202,16 @@ void invalidate_graph(H* h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
     h->gkey.clear();
+    if (h->gexec_io) cudaGraphExecDestroy(h->gexec_io);
+    h->gexec_io = nullptr;
+    h->gkey_io.clear();
 }
+
+// Host state of gbsph_fluid3d_compute_host: three float4[n] inputs and outputs.
+struct HostIO {
+    const float* in[3];
+    float* out[3];
+};
 
 void free_particle_arrays(H* h) {
     if (h->pblock) cudaFree(h->pblock);
@@ -284,7 +298,7 @@ int st_hash(H* h, const KParams& kp, cudaStream_t s, bool clear) {
     return GBSPH_OK;
 }
 
-int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather) {
+int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather, cudaEvent_t before_last = nullptr) {
     OnesweepArgs a;
     a.keys_in = h->keys_a;
     a.vals_in = nullptr;
@@ -306,6 +320,7 @@ int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather) {
         a.gather.dst[0] = h->spos;
         a.gather.dst[1] = h->svel;
     }
+    a.before_last = before_last;
     GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
     return GBSPH_OK;
 }
@@ -430,18 +445,32 @@ int mark(H* h, int i, cudaStream_t s) {
     return GBSPH_OK;
 }
 
-// The fused step (default).
-int enqueue_fused(H* h, const KParams& kp, cudaStream_t s) {
+// The fused step (default). With `io` the step also uploads its state from host memory and
+// downloads it after: position first on `s`; velocity and force on a side stream, waited for
+// just before the sort's last pass (which gathers velocities) and before the force pass, so
+// their transfers overlap the hash, the sort and the density pass; the three downloads follow
+// the force pass.
+int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nullptr) {
     const bool linear = kp.key_mode == GBSPH_KEY_LINEAR_GRID;
     const bool clear = linear && h->table_clean;
+    const size_t bytes = (size_t)kp.n * 16;
     h->ev_valid = false;
+    if (io) {
+        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[0], s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(h->io_stream, h->io_ev[0], 0));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 1), io->in[1], bytes, cudaMemcpyHostToDevice, h->io_stream));
+        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[1], h->io_stream));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 2), io->in[2], bytes, cudaMemcpyHostToDevice, h->io_stream));
+        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[2], h->io_stream));
+        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 0), io->in[0], bytes, cudaMemcpyHostToDevice, s));
+    }
     RC(mark(h, 0, s));
     if (linear && !h->table_clean)
         GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->table_cells * sizeof(uint2), s));
     h->table_clean = false;
     RC(st_hash(h, kp, s, clear));
     RC(mark(h, 1, s));
-    RC(st_sort(h, kp, s, true));
+    RC(st_sort(h, kp, s, true, io ? h->io_ev[1] : nullptr));
     RC(mark(h, 2, s));
     if (linear) {
         // counters were zeroed with the sort scratch in st_hash
@@ -451,12 +480,14 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s) {
         RC(mark(h, 3, s));
         RC(st_density_brick(h, kp, s));
         RC(mark(h, 4, s));
+        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
         RC(st_force_brick(h, kp, s, h->hook == nullptr));
     } else {
         RC(st_bounds(h, kp, s, true));
         RC(mark(h, 3, s));
         RC(st_density_exact(h, kp, s));
         RC(mark(h, 4, s));
+        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
         RC(st_forces_exact(h, kp, s));
         if (!h->hook) {
             k_post_fused<<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2), kp);
@@ -465,7 +496,10 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s) {
     }
     RC(mark(h, 5, s));
     h->ev_valid = h->opt_profile != 0;
-    if (h->hook) return run_hook(h, s);
+    if (h->hook) RC(run_hook(h, s));
+    if (io)
+        for (int w = 0; w < 3; w++)
+            GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(io->out[w], P4(h, w), bytes, cudaMemcpyDeviceToHost, s));
     return GBSPH_OK;
 }
 
@@ -590,6 +624,9 @@ GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h) {
     if (h->table) cudaFree(h->table);
     if (h->err) cudaFree(h->err);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    if (h->io_stream) cudaStreamDestroy(h->io_stream);
+    for (auto e : h->io_ev)
+        if (e) cudaEventDestroy(e);
     for (auto e : h->ev)
         if (e) cudaEventDestroy(e);
     delete h;
@@ -701,26 +738,46 @@ GBSPH_API int gbsph_fluid3d_stage_times(gbsph_fluid3d_t h, float* ms, int max_st
     return n;
 }
 
-GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream) {
-    if (!h) return GBSPH_ERR_ARGUMENT;
-    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "compute() before compile()");
+namespace {
+
+// One step on `s`; with `io` (compute_host) the upload and download are part of it. The
+// default path replays a captured graph (one per kind: with and without host copies).
+int compute_impl(H* h, cudaStream_t s, const HostIO* io, bool io_graph) {
     RC(validate_params(h));
     GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
     RC(ensure_tables(h));
     const KParams kp = make_kparams(h);
-    cudaStream_t s = (cudaStream_t)stream;
-    if (!h->opt_fused) return enqueue_staged(h, kp, s);
+    const size_t bytes = (size_t)kp.n * 16;
+    if (!h->opt_fused) {
+        if (io)
+            for (int w = 0; w < 3; w++)
+                GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, w), io->in[w], bytes, cudaMemcpyHostToDevice, s));
+        RC(enqueue_staged(h, kp, s));
+        if (io)
+            for (int w = 0; w < 3; w++)
+                GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(io->out[w], P4(h, w), bytes, cudaMemcpyDeviceToHost, s));
+        return GBSPH_OK;
+    }
     const bool steady = kp.key_mode != GBSPH_KEY_LINEAR_GRID || h->table_clean;
-    if (h->hook || !h->opt_graph || !steady || h->opt_profile) {
-        const int rc = enqueue_fused(h, kp, s);
+    if (h->hook || !h->opt_graph || !steady || h->opt_profile || (io && !io_graph)) {
+        const int rc = enqueue_fused(h, kp, s, io);
         if (rc) h->table_clean = false;
         return rc;
     }
     std::vector<char> key = graph_key(h, kp);
-    if (!h->gexec || key != h->gkey) {
-        invalidate_graph(h);
+    if (io) {
+        const size_t o = key.size();
+        key.resize(o + sizeof(HostIO));
+        std::memcpy(key.data() + o, io, sizeof(HostIO));
+    }
+    cudaGraphExec_t& gexec = io ? h->gexec_io : h->gexec;
+    std::vector<char>& gkey = io ? h->gkey_io : h->gkey;
+    if (!gexec || key != gkey) {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        gkey.clear();
         GBSPH_CUDA_TRY(&h->last_error, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_fused(h, kp, h->cap_stream);
+        const int rc = enqueue_fused(h, kp, h->cap_stream, io);
         cudaGraph_t g = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
         if (rc || ce != cudaSuccess) {
@@ -728,22 +785,57 @@ GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream) {
             h->table_clean = false;
             return rc ? rc : fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
         }
-        const cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
+        const cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) {
-            h->gexec = nullptr;
+            gexec = nullptr;
             h->table_clean = false;
             return fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
         }
-        h->gkey = key;
+        gkey = key;
     }
-    const cudaError_t le = cudaGraphLaunch(h->gexec, s);
+    const cudaError_t le = cudaGraphLaunch(gexec, s);
     if (le != cudaSuccess) {
         h->table_clean = false;
         return fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(le));
     }
     h->table_clean = true;
     return GBSPH_OK;
+}
+
+bool is_pinned_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
+GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "compute() before compile()");
+    return compute_impl(h, (cudaStream_t)stream, nullptr, false);
+}
+
+GBSPH_API int gbsph_fluid3d_compute_host(gbsph_fluid3d_t h, const float* position_in, const float* velocity_in,
+                                         const float* force_in, float* position_out, float* velocity_out,
+                                         float* force_out, void* stream) {
+    if (!h) return GBSPH_ERR_ARGUMENT;
+    if (!h->compiled) return fail(&h->last_error, GBSPH_ERR_NOT_COMPILED, "compute() before compile()");
+    if (!position_in || !velocity_in || !force_in || !position_out || !velocity_out || !force_out)
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "null host buffer");
+    GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
+    if (!h->io_stream) {
+        GBSPH_CUDA_TRY(&h->last_error, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
+        for (auto& e : h->io_ev) GBSPH_CUDA_TRY(&h->last_error, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const HostIO io{{position_in, velocity_in, force_in}, {position_out, velocity_out, force_out}};
+    bool pinned = true;
+    for (int w = 0; w < 3; w++) pinned = pinned && is_pinned_host(io.in[w]) && is_pinned_host(io.out[w]);
+    return compute_impl(h, (cudaStream_t)stream, &io, pinned);
 }
 
 GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream) {

@@ -84,6 +84,7 @@ struct OnesweepArgs {
     void* scratch = nullptr;
     uint32_t* err = nullptr;
     SortGather gather;
+    cudaEvent_t before_last = nullptr;  // if set: the last pass waits for it (its gather's inputs)
 };
 
 // Zeroes the scratch header and the look-back words.

@@ -345,6 +345,10 @@ cudaError_t onesweep_passes(const OnesweepArgs& a, cudaStream_t s) {
         const int shift = a.start_bit + p * SORT_RADIX_BITS;
         const int bits = std::min(SORT_RADIX_BITS, a.end_bit - shift);
         const int ng = last ? a.gather.n_gather : 0;
+        if (last && a.before_last) {
+            cudaError_t e = cudaStreamWaitEvent(s, a.before_last, 0);
+            if (e != cudaSuccess) return e;
+        }
         cudaError_t e = (vin == nullptr)
             ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s)
             : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s);
