@@ -173,6 +173,14 @@ class gbFluid3D {
         mDevice = &dev;
         return ok(gbsph_fluid3d_compute(mH, dev.getQueue()));
     }
+    // One step on host-resident float4 state (page-locked memory for the overlapped path):
+    // the inputs are uploaded, the step runs, the outputs (may be the inputs) are downloaded;
+    // asynchronous on dev's queue.
+    int computeHost(gbDevice& dev, const float* pos, const float* vel, const float* force, float* posOut,
+                    float* velOut, float* forceOut) {
+        mDevice = &dev;
+        return ok(gbsph_fluid3d_compute_host(mH, pos, vel, force, posOut, velOut, forceOut, dev.getQueue()));
+    }
     // One reference stage (GBSPH_STAGE_*), e.g. from an EVT_INTEGRATE handler.
     int stage(int which) { return ok(gbsph_fluid3d_stage(mH, which, mDevice ? mDevice->getQueue() : nullptr)); }
 

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 
 #include "gbFluid3D.hpp"
 
@@ -93,6 +94,31 @@ static int testFluid3D0(gbContext& ctx) {
     CHECK(sp.map(gbBuffer::MAP_READ));
     for (size_t i = 0; i < fluid.getParticleCount(); i++) CHECK(sp.ptr<float>()[4 * i + 3] >= 1.0f);  // density
     std::printf("testFluid3D0: average particle position = %g %g %g\n", avg[0], avg[1], avg[2]);
+    // a step from page-locked host state (computeHost) equals the same step on device buffers
+    const size_t n = fluid.getParticleCount();
+    float *in = nullptr, *out = nullptr;
+    CHECK(cudaHostAlloc((void**)&in, 3 * n * 16, cudaHostAllocDefault) == cudaSuccess);
+    CHECK(cudaHostAlloc((void**)&out, 3 * n * 16, cudaHostAllocDefault) == cudaSuccess);
+    gbBuffer* bufs[3] = {fluid.getPositionBuffer(), fluid.getVelocityBuffer(), fluid.getForceBuffer()};
+    for (int k = 0; k < 3; k++) {
+        CHECK(bufs[k]->map(gbBuffer::MAP_READ));
+        std::memcpy(in + 4 * n * k, bufs[k]->ptr<float>(), n * 16);
+    }
+    CHECK(fluid.computeHost(dev, in, in + 4 * n, in + 8 * n, out, out + 4 * n, out + 8 * n));
+    cudaDeviceSynchronize();
+    for (int k = 0; k < 3; k++) {  // back to the state before the step, then the device step
+        CHECK(bufs[k]->map(gbBuffer::MAP_WRITE));
+        std::memcpy(bufs[k]->ptr<float>(), in + 4 * n * k, n * 16);
+        CHECK(bufs[k]->unmap());
+    }
+    CHECK(fluid.compute(dev));
+    cudaDeviceSynchronize();
+    for (int k = 0; k < 3; k++) {
+        CHECK(bufs[k]->map(gbBuffer::MAP_READ));
+        CHECK(std::memcmp(out + 4 * n * k, bufs[k]->ptr<float>(), n * 16) == 0);
+    }
+    cudaFreeHost(in);
+    cudaFreeHost(out);
     return 0;
 }
 
