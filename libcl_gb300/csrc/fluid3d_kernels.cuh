@@ -758,8 +758,12 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                 uint32_t nk = 0;  // in-range candidates of this lane (the target itself included)
                 if (active && staged) {
                     // 32-bit shared-memory addresses stepped per candidate: the candidate's
-                    // position (16 bytes) and this lane's next list slot.
-                    const uint32_t my_a = smem_addr(my), last = sub - 1u, step = Q * 16u;
+                    // position (16 bytes) and this lane's next list slot, wa, which stops one
+                    // slot past the sub-list (the next lane's first slot, or the row's padding).
+                    // A lane that gets there has overflowed (nk = sub): its target is then
+                    // scanned by the force pass and none of its sub-lists is read.
+                    const uint32_t my_a = smem_addr(my), w_end = my_a + 2u * sub, step = Q * 16u;
+                    uint32_t wa = my_a;
 #pragma unroll 1
                     for (int r = 0; r < R; ++r) {
                         const uint32_t lo = S.off[r][c], len = S.off[r][c + 3] - lo;
@@ -779,14 +783,13 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                             const float tt = in ? h2 - r2 : 0.0f;
                             acc = fmaf(tt * tt, tt, acc);
                             // branch-free append: the slot after the last real entry is
-                            // overwritten by the next candidate.
-                            // Once the sub-list is full, later candidates overwrite its last
-                            // entry, so a full sub-list counts as an overflow. The target and
-                            // coincident particles (r^2 = 0) are listed; the force pass skips them.
-                            sts_u16(my_a + 2u * min(nk, last), v);
-                            nk += in ? 1u : 0u;
+                            // overwritten by the next candidate. The target and coincident
+                            // particles (r^2 = 0) are listed; the force pass skips them.
+                            sts_u16(wa, v);
+                            wa = min(wa + (in ? 2u : 0u), w_end);
                         }
                     }
+                    nk = (wa - my_a) >> 1;  // at most sub: an overflowed lane counts sub
                 } else if (active) {  // unstaged brick: candidates from global memory, no lists
 #pragma unroll 1
                     for (int r = 0; r < R; ++r) {
@@ -1031,18 +1034,18 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
             const uint32_t gi = S.lo[RC] + tl;
             float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
             float4 pi = make_float4(0.f, 0.f, 0.f, 0.f), vi = pi, f_o = pi, v_o = pi, p_o = pi;
-            uint32_t o = 0;
+            uint32_t o = 0, Q = 0, sub = 0, c = 0;
+            uint64_t meta = NBR_SCAN;
             if (active) {
                 // the target's cell and its place in the density pass's groups (its sub-lists)
-                int c = 0;
-                while (c + 1 < ncell && S.off[RC][c + 2] <= tl) ++c;
+                while (c + 1 < (uint32_t)ncell && S.off[RC][c + 2] <= tl) ++c;
                 const uint32_t c0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - c0;
                 const uint32_t g0 = (tl - c0) & ~(GROUP_MAX - 1u);
                 const uint32_t f = L.info[min(GROUP_MAX, nt - g0)];
-                const uint32_t Q = f & 0xFFu, sub = f >> 8;
+                Q = f & 0xFFu;
+                sub = f >> 8;
                 pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
                 vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
-                const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
                 if (p == 0) {  // prefetch what the integration needs
                     o = (staged && lists_staged) ? s_index[gi - (tfirst & ~3u)] : index[gi];
                     f_o = force[o];
@@ -1051,19 +1054,46 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                         p_o = pos[o];
                     }
                 }
-                const uint64_t meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
-                const bool scan = (meta & NBR_SCAN) != 0;
+                meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
+            }
+            const bool scan = (meta & NBR_SCAN) != 0;
+            const bool whole = (Q % P) == 0 && (sub & 7u) == 0;
+            // The chunk walk below serves targets whose sub-lists start on 16-byte chunks and
+            // pair up (Q = 2, 4, 8). A warp whose listed targets are not all of that kind
+            // walks every listed target's entries as one sequence instead, so that its lanes
+            // run the same loop whatever each target's sub-list layout.
+            const bool chunked = __all_sync(0xffffffffu, scan || whole);
+            if (active) {
+                const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
                 if (!scan) {
-                    // When the sub-lists start on 16-byte chunks and pair up (Q = 2, 4, 8),
-                    // lane p walks sub-lists p, p + 2, ... chunk by chunk; otherwise the Q
-                    // sub-lists are one sequence and lane p takes its entries p, p + 2, ...,
-                    // two at a time so that their loads overlap (slot s of the target's list
-                    // sits at chunk-major position ((s >> 3) * ntarg + u) * 8 + (s & 7))
+                    // Slot s of the target's list sits at chunk-major position
+                    // ((s >> 3) * ntarg + u) * 8 + (s & 7).
                     const uint16_t* lst = (lists_staged ? s_lists : nbr + (size_t)tfirst * NBR_CAP) + (gi - tfirst) * 8u;
                     const uint32_t n8 = ntarg * 8u;
-                    uint32_t before = 0;  // entries of the earlier sub-lists
-                    const bool whole = (Q % P) == 0 && (sub & 7u) == 0;
-                    if (whole) {
+                    if (!chunked) {
+                        // lane p takes entries p, p + P, ... of the concatenated sub-lists:
+                        // (q, k) is the current entry's sub-list and place in it
+                        const uint32_t n = (uint32_t)((meta * 0x0101010101010101ull) >> 56);
+                        uint32_t q = 0, k = p, nq = (uint32_t)meta & 127u;
+                        while (k >= nq && q + 1 < Q) {
+                            k -= nq;
+                            ++q;
+                            nq = (uint32_t)(meta >> (8 * q)) & 127u;
+                        }
+#pragma unroll 1
+                        for (uint32_t e = p; e < n; e += P) {
+                            const uint32_t s = q * sub + k;
+                            const uint32_t i0 = lst[(s >> 3) * n8 + (s & 7u)];
+                            force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
+                            k += P;
+                            while (k >= nq && q + 1 < Q) {
+                                k -= nq;
+                                ++q;
+                                nq = (uint32_t)(meta >> (8 * q)) & 127u;
+                            }
+                        }
+                    } else {
+                        // lane p walks sub-lists p, p + 2, ... chunk by chunk
 #pragma unroll 1
                         for (uint32_t q = p; q < Q; q += P) {
                             const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u;
@@ -1080,24 +1110,6 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                                 }
                             }
                         }
-                    }
-#pragma unroll 1
-                    for (uint32_t q = 0; q < (whole ? 0u : Q); ++q) {
-                        const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u, b = q * sub;
-                        uint32_t k = (p - before) & (P - 1u);
-                        for (; k + P < n; k += 2 * P) {
-                            const uint32_t s0 = b + k, s1 = s0 + P;
-                            const uint32_t i0 = lst[(s0 >> 3) * n8 + (s0 & 7u)];
-                            const uint32_t i1 = lst[(s1 >> 3) * n8 + (s1 & 7u)];
-                            force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
-                            force_pair_pre<DIMS>(pi, vi, s_pos[i1], s_vel[i1], kp.h, acc);
-                        }
-                        if (k < n) {
-                            const uint32_t s0 = b + k;
-                            const uint32_t i0 = lst[(s0 >> 3) * n8 + (s0 & 7u)];
-                            force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
-                        }
-                        before += n;
                     }
                 } else {
 #pragma unroll 1
