@@ -955,7 +955,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
     extern __shared__ float4 s_buf[];
     __shared__ BrickShared S;
     __shared__ LaneMap L;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int t = threadIdx.x, lane = t & 31;
     lane_map_init(L);
     if (t == 0) {
         mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
@@ -1057,43 +1057,51 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                 meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
             }
             const bool scan = (meta & NBR_SCAN) != 0;
+            // Sub-lists that start on 16-byte chunks and pair up (Q = 2, 4, 8) can be walked a
+            // chunk at a time; a warp whose listed targets are all of that kind does so. Any
+            // other warp walks every listed target in one flat loop (the same loop for every
+            // layout, so that its lanes stay together). Both visit a target's entries in the
+            // same order, which depends on the target's own sub-lists only: with Q even lane p
+            // takes sub-lists p, p + 2, ... whole, otherwise entries p, p + 2, ... of the
+            // concatenated sub-lists.
             const bool whole = (Q % P) == 0 && (sub & 7u) == 0;
-            // The chunk walk below serves targets whose sub-lists start on 16-byte chunks and
-            // pair up (Q = 2, 4, 8). A warp whose listed targets are not all of that kind
-            // walks every listed target's entries as one sequence instead, so that its lanes
-            // run the same loop whatever each target's sub-list layout.
             const bool chunked = __all_sync(0xffffffffu, scan || whole);
             if (active) {
                 const float inv_rho_i = staged ? pi.w : 1.0f / pi.w;
                 if (!scan) {
-                    // Slot s of the target's list sits at chunk-major position
-                    // ((s >> 3) * ntarg + u) * 8 + (s & 7).
+                    // slot s of the target's list sits at chunk-major position
+                    // ((s >> 3) * ntarg + u) * 8 + (s & 7)
                     const uint16_t* lst = (lists_staged ? s_lists : nbr + (size_t)tfirst * NBR_CAP) + (gi - tfirst) * 8u;
                     const uint32_t n8 = ntarg * 8u;
                     if (!chunked) {
-                        // lane p takes entries p, p + P, ... of the concatenated sub-lists:
-                        // (q, k) is the current entry's sub-list and place in it
-                        const uint32_t n = (uint32_t)((meta * 0x0101010101010101ull) >> 56);
-                        uint32_t q = 0, k = p, nq = (uint32_t)meta & 127u;
-                        while (k >= nq && q + 1 < Q) {
-                            k -= nq;
-                            ++q;
-                            nq = (uint32_t)(meta >> (8 * q)) & 127u;
+                        // (q, k): the next entry's sub-list and place in it; m: the lane's count
+                        const bool pairs = (Q % P) == 0;
+                        const uint32_t dq = pairs ? P : 1u, dk = pairs ? 1u : P;
+                        uint32_t q = pairs ? p : 0u, k = pairs ? 0u : p, m;
+                        if (pairs) {  // bytes p, p + 2, ... of meta
+                            m = (uint32_t)(((meta & (0x00FF00FF00FF00FFull << (8 * p))) * 0x0101010101010101ull) >> 56);
+                        } else {
+                            const uint32_t n = (uint32_t)((meta * 0x0101010101010101ull) >> 56);
+                            m = n > p ? (n - p + P - 1u) / P : 0u;
                         }
+                        uint32_t nq = (uint32_t)(meta >> (8 * q)) & 127u;
+                        auto settle = [&]() {
+                            while (k >= nq && q + dq < Q) {
+                                k -= nq;
+                                q += dq;
+                                nq = (uint32_t)(meta >> (8 * q)) & 127u;
+                            }
+                        };
+                        settle();
 #pragma unroll 1
-                        for (uint32_t e = p; e < n; e += P) {
+                        for (uint32_t i = 0; i < m; ++i) {
                             const uint32_t s = q * sub + k;
                             const uint32_t i0 = lst[(s >> 3) * n8 + (s & 7u)];
                             force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
-                            k += P;
-                            while (k >= nq && q + 1 < Q) {
-                                k -= nq;
-                                ++q;
-                                nq = (uint32_t)(meta >> (8 * q)) & 127u;
-                            }
+                            k += dk;
+                            settle();
                         }
                     } else {
-                        // lane p walks sub-lists p, p + 2, ... chunk by chunk
 #pragma unroll 1
                         for (uint32_t q = p; q < Q; q += P) {
                             const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u;
@@ -1111,11 +1119,11 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                             }
                         }
                     }
-                } else {
+                } else if (!staged) {  // unstaged brick: both lanes scan the rows in global memory
 #pragma unroll 1
                     for (int r = 0; r < R; ++r) {
-                        const float4* rp = staged ? s_pos + S.base[r] : spos + S.lo[r];
-                        const float4* rv = staged ? s_vel + S.base[r] : svel + S.lo[r];
+                        const float4* rp = spos + S.lo[r];
+                        const float4* rv = svel + S.lo[r];
                         const uint32_t hi = S.off[r][c + 3];
                         for (uint32_t j = S.off[r][c] + p; j < hi; j += P) {
                             const float4 pj = rp[j];
@@ -1125,11 +1133,48 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                                 const float dz = pi.z - pj.z;
                                 r2 = fmaf(dz, dz, r2);
                             }
-                            if (r2 < kp.r2_thresh && r2 > 0.0f) {
-                                if (staged) force_pair_pre<DIMS>(pi, vi, pj, rv[j], kp.h, acc);
-                                else force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
-                            }
+                            if (r2 < kp.r2_thresh && r2 > 0.0f) force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
                         }
+                    }
+                }
+            }
+            if (staged) {
+                // Targets of a staged brick whose sub-lists overflowed: the whole warp scans
+                // each one's rows in turn (lane l takes candidates l, l + 32, ... of every
+                // row) and the sum goes to the target's first lane.
+                uint32_t pend = __ballot_sync(0xffffffffu, active && scan && p == 0);
+                while (pend) {
+                    const int src = __ffs(pend) - 1;
+                    pend &= pend - 1u;
+                    const float4 ps = make_float4(__shfl_sync(0xffffffffu, pi.x, src), __shfl_sync(0xffffffffu, pi.y, src),
+                                                  __shfl_sync(0xffffffffu, pi.z, src), __shfl_sync(0xffffffffu, pi.w, src));
+                    const float4 vs = make_float4(__shfl_sync(0xffffffffu, vi.x, src), __shfl_sync(0xffffffffu, vi.y, src),
+                                                  __shfl_sync(0xffffffffu, vi.z, src), __shfl_sync(0xffffffffu, vi.w, src));
+                    const uint32_t cs = __shfl_sync(0xffffffffu, c, src);
+                    float a[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+                    for (int r = 0; r < R; ++r) {
+                        const float4* rp = s_pos + S.base[r];
+                        const float4* rv = s_vel + S.base[r];
+                        const uint32_t hi = S.off[r][cs + 3];
+                        for (uint32_t j = S.off[r][cs] + (uint32_t)lane; j < hi; j += 32) {
+                            const float4 pj = rp[j];
+                            const float dx = ps.x - pj.x, dy = ps.y - pj.y;
+                            float r2 = fmaf(dy, dy, dx * dx);
+                            if (DIMS == 3) {
+                                const float dz = ps.z - pj.z;
+                                r2 = fmaf(dz, dz, r2);
+                            }
+                            if (r2 < kp.r2_thresh) force_pair_pre<DIMS>(ps, vs, pj, rv[j], kp.h, a);
+                        }
+                    }
+                    for (int m = 16; m > 0; m >>= 1) {
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) a[k] += __shfl_xor_sync(0xffffffffu, a[k], m);
+                    }
+                    if (lane == src) {
+#pragma unroll
+                        for (int k = 0; k < 6; ++k) acc[k] = a[k];
                     }
                 }
             }

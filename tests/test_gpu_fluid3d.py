@@ -9,7 +9,7 @@ import oracle
 from fluid_helpers import RTOL, hash_block, make_fluid, perturbed, pos_err, rel_err, set_params, sorted_outputs, state
 from libcl_gb300 import (ERR_ARGUMENT, ERR_NOT_COMPILED, ERR_SIZE_MISMATCH, OK, OPT_BRICK_WIDTH, REF_BUCKETS,
                          STAGE_GRAVITY, STAGE_INTEGRATE_FORCE, STAGE_INTEGRATE_VELOCITY, Fluid3D)
-from libcl_gb300.scenes import block_collapse_3d, clone_params, reference_test_scene
+from libcl_gb300.scenes import block_collapse_3d, clone_params, lattice, reference_test_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -144,6 +144,34 @@ def test_brick_width_does_not_change_results(cuda, bw):
     sa, sb = state(a), state(b)
     for k in sa:
         assert_bit_exact(sa[k], sb[k], k)
+
+
+def disordered_block(nx=48, ny=24, nz=48, seed=11):
+    """The block collapse's lattice jittered by up to one spacing (half a cell) per axis, so
+    cells hold anything from a few to a dozen or more particles: the neighbour passes see
+    every group size, sub-list layout (Q = 2 ... 8) and some overflowing sub-lists."""
+    sc = block_collapse_3d(nx, ny, nz)
+    sc.pos = lattice(nx, ny, nz, 0.01, (0.015, 0.015, 0.015), 0.01, seed)
+    return sc
+
+
+def test_disordered_block_within_tolerance_and_brick_width_free(cuda):
+    sc = disordered_block()
+    vel = perturbed(sc, sigma=0.2)
+    a = make_fluid(sc, fused=True, vel=vel)
+    a.compute()
+    g, gs = sorted_outputs(a, oracle.table_cells(sc.params)), state(a)
+    occ = np.unique(np.bincount(g["cell"].astype(np.int64)))
+    assert len(occ) >= 8, occ  # the groups really vary (occupancies 0 ... 12 and more)
+    r, rs = oracle_step(sc, vel)
+    compare_fast(g, gs, r, rs, sc.pos)
+    for bw in (1, 5, 8):
+        b = make_fluid(sc, fused=True, vel=vel)
+        b.set_option(OPT_BRICK_WIDTH, bw)
+        b.compute()
+        sb = state(b)
+        for k in gs:
+            assert_bit_exact(gs[k], sb[k], f"{k} (brick width {bw})")
 
 
 def test_integrate_hook(cuda):
