@@ -1022,9 +1022,9 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
         }
         // P = 2 lanes per target: the brick's targets are consecutive in the centre row, so the
         // CTA takes 128 of them at a time whatever cell they are in; the two lanes of a target
-        // split its list (or, scanning, take alternate candidates of each row) and their
-        // partial sums are added with a shuffle. The summation order depends on neither the
-        // brick width nor the brick's target count.
+        // split its list (or, in an unstaged brick, take alternate candidates of each row) and
+        // their partial sums are added with a shuffle. The summation order depends on neither
+        // the brick width nor the brick's target count, as long as the brick is staged.
         const uint32_t tbeg = S.off[RC][1];
         constexpr uint32_t lp = 1u, P = 1u << lp;
         for (uint32_t u0 = 0; u0 < ntarg; u0 += BRICK_THREADS >> lp) {
