@@ -158,7 +158,7 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     a.gather.dst[0] = h->spos;
     a.gather.dst[1] = h->svel;
     GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
-    k_bounds_batch<<<(kp.n + 255) / 256, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, bcounters(h), h->err);
+    k_bounds_batch<<<(kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, bcounters(h), h->err);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     h->table_clean = true;
     k_density_brick<3, true><<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks,

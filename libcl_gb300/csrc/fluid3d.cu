@@ -335,7 +335,7 @@ int st_bounds(H* h, const KParams& kp, cudaStream_t s, bool full_clear) {
     if (kp.key_mode == GBSPH_KEY_LINEAR_GRID) {
         if (full_clear) GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->table_cells * sizeof(uint2), s));
         GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(counters(h), 0, 16, s));
-        k_bounds_linear<<<grid1(kp.n), 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
+        k_bounds_linear<<<(kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
         GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     } else {
         GBSPH_CUDA_TRY(&h->last_error, cell_bounds_launch(h->keys_c, kp.n, h->hash_tables,
@@ -474,7 +474,7 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
     RC(mark(h, 2, s));
     if (linear) {
         // counters were zeroed with the sort scratch in st_hash
-        k_bounds_linear<<<grid1(kp.n), 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
+        k_bounds_linear<<<(kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
         GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
         h->table_clean = true;
         RC(mark(h, 3, s));

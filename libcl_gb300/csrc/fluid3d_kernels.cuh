@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos, KP
         for (int p = 0; p < passes; ++p) {
             const int shift = p * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
-            atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
+            hist_add(s_h, p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u)));
         }
         if (CLEAR) {
             const uint32_t pk = prev_keys[i];
@@ -153,26 +153,57 @@ static __global__ void k_reorder(const uint32_t* __restrict__ index, const float
     svel[i] = vel[s];
 }
 
-// Cell bounds into the interleaved LINEAR_GRID table, plus the list of occupied bricks
-// (brick id = x/W + bxn*(y + ny*z)), appended through an atomic counter.
-static __global__ void k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
-                                uint2* __restrict__ table, uint32_t* __restrict__ bricks,
-                                uint32_t* __restrict__ n_bricks, uint32_t* err) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp.n) return;
-    const uint32_t k = keys[i];
-    if (k >= kp.table_cells) {
-        atomicOr(err, DEV_ERR_KEY_RANGE);
-        return;
+// Cell bounds into the interleaved LINEAR_GRID table, plus the list of occupied bricks,
+// for BOUNDS_TILE consecutive sorted keys per CTA (BOUNDS_ITEMS per thread, strided by the
+// block). A key that starts a cell writes the cell's first index, one that ends it the end;
+// a key whose brick differs from its predecessor's appends the brick id: the CTA's appends
+// take ranks from a shared counter and reserve their slots with one global atomic (one
+// counter address, so per-key atomics would queue behind each other).
+constexpr uint32_t BOUNDS_ITEMS = 4;
+constexpr uint32_t BOUNDS_TILE = 256 * BOUNDS_ITEMS;
+
+template <class BrickOf>
+__device__ __forceinline__ void bounds_tile(const uint32_t* __restrict__ keys, const KParams& kp,
+                                            uint2* __restrict__ table, uint32_t* __restrict__ bricks,
+                                            uint32_t* __restrict__ n_bricks, uint32_t* err, BrickOf brick_of) {
+    __shared__ uint32_t s_cnt, s_base;
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    uint32_t bid[BOUNDS_ITEMS], rank[BOUNDS_ITEMS];
+    const uint32_t i0 = blockIdx.x * BOUNDS_TILE + threadIdx.x;
+#pragma unroll
+    for (uint32_t it = 0; it < BOUNDS_ITEMS; ++it) {
+        const uint32_t i = i0 + it * blockDim.x;
+        rank[it] = EMPTY;
+        bid[it] = 0;
+        if (i >= kp.n) continue;
+        const uint32_t k = keys[i];
+        if (k >= kp.table_cells) {
+            atomicOr(err, DEV_ERR_KEY_RANGE);
+            continue;
+        }
+        const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
+        const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
+        if (k != prev) table[k].x = i;
+        if (k != next) table[k].y = i + 1;
+        bid[it] = brick_of(k);
+        if (prev == EMPTY || bid[it] != brick_of(prev)) rank[it] = atomicAdd(&s_cnt, 1u);
     }
-    const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
-    const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
-    if (k != prev) table[k].x = i;
-    if (k != next) table[k].y = i + 1;
-    const uint32_t nx = (uint32_t)kp.nx, bw = (uint32_t)kp.bw;
-    const uint32_t bid = (k % nx) / bw + (uint32_t)kp.bxn * (k / nx);
-    const uint32_t pbid = (prev == EMPTY) ? EMPTY : (prev % nx) / bw + (uint32_t)kp.bxn * (prev / nx);
-    if (bid != pbid) bricks[atomicAdd(n_bricks, 1u)] = bid;
+    __syncthreads();
+    if (threadIdx.x == 0 && s_cnt) s_base = atomicAdd(n_bricks, s_cnt);
+    __syncthreads();
+#pragma unroll
+    for (uint32_t it = 0; it < BOUNDS_ITEMS; ++it)
+        if (rank[it] != EMPTY) bricks[s_base + rank[it]] = bid[it];
+}
+
+// Single scene: brick id = x/W + bxn*(y + ny*z).
+static __global__ void __launch_bounds__(256) k_bounds_linear(const uint32_t* __restrict__ keys, KParams kp,
+                                                              uint2* __restrict__ table, uint32_t* __restrict__ bricks,
+                                                              uint32_t* __restrict__ n_bricks, uint32_t* err) {
+    const uint32_t nx = (uint32_t)kp.nx, bw = (uint32_t)kp.bw, bxn = (uint32_t)kp.bxn;
+    bounds_tile(keys, kp, table, bricks, n_bricks, err,
+                [=](uint32_t k) { return (k % nx) / bw + bxn * (k / nx); });
 }
 
 // Batch version of k_hash: each particle keys into its own scene's grid; the key is the
@@ -197,7 +228,7 @@ __global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ p
         for (int q = 0; q < passes; ++q) {
             const int shift = q * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
-            atomicAdd(&s_h[q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
+            hist_add(s_h, q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u)));
         }
         if (CLEAR) {
             const uint32_t pk = prev_keys[i];
@@ -216,22 +247,10 @@ __device__ __forceinline__ uint32_t batch_brick_of(const KParams& kp, uint32_t k
 }
 
 // Batch version of k_bounds_linear: brick ids are global (scene brick offset + local id).
-static __global__ void k_bounds_batch(const uint32_t* __restrict__ keys, KParams kp, uint2* __restrict__ table,
-                               uint32_t* __restrict__ bricks, uint32_t* __restrict__ n_bricks, uint32_t* err) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kp.n) return;
-    const uint32_t k = keys[i];
-    if (k >= kp.table_cells) {
-        atomicOr(err, DEV_ERR_KEY_RANGE);
-        return;
-    }
-    const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
-    const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
-    if (k != prev) table[k].x = i;
-    if (k != next) table[k].y = i + 1;
-    const uint32_t bid = batch_brick_of(kp, k);
-    const uint32_t pbid = prev == EMPTY ? EMPTY : batch_brick_of(kp, prev);
-    if (bid != pbid) bricks[atomicAdd(n_bricks, 1u)] = bid;
+static __global__ void __launch_bounds__(256) k_bounds_batch(const uint32_t* __restrict__ keys, KParams kp,
+                                                             uint2* __restrict__ table, uint32_t* __restrict__ bricks,
+                                                             uint32_t* __restrict__ n_bricks, uint32_t* err) {
+    bounds_tile(keys, kp, table, bricks, n_bricks, err, [&](uint32_t k) { return batch_brick_of(kp, k); });
 }
 
 // Splits the interleaved table into two arrays (for inspection through the ABI).
