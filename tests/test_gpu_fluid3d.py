@@ -401,6 +401,30 @@ def test_dam_break_2d_fused_steps_fed_identical_state(cuda):
     assert f.sync_status() == OK
 
 
+def test_disordered_2d_block_within_tolerance_and_brick_width_free(cuda):
+    """dims = 2 on the brick kernels with the dam break's lattice jittered by up to one spacing
+    per axis: cells hold 0 to 9 particles, so every 2D group size and sub-list layout occurs."""
+    from libcl_gb300.scenes import dam_break_2d
+    sc = dam_break_2d()
+    sc.pos = lattice(128, 128, 1, 0.005, (0.01, 0.01, 0.0), 0.005, 12)
+    sc.pos[:, 2] = 0.0
+    vel = perturbed(sc, sigma=0.2)
+    vel[:, 2] = 0.0
+    a = make_fluid(sc, fused=True, vel=vel)
+    a.compute()
+    g, gs = sorted_outputs(a, oracle.table_cells(sc.params)), state(a)
+    assert len(np.unique(np.bincount(g["cell"].astype(np.int64)))) >= 7
+    r, rs = oracle_step(sc, vel)
+    compare_fast(g, gs, r, rs, sc.pos)
+    for bw in (1, 6):
+        b = make_fluid(sc, fused=True, vel=vel)
+        b.set_option(OPT_BRICK_WIDTH, bw)
+        b.compute()
+        sb = state(b)
+        for k in gs:
+            assert_bit_exact(gs[k], sb[k], f"{k} (brick width {bw})")
+
+
 def test_emitter(cuda):
     """clEmitter (libCL/phys/oclFluid3D.cl:273-282): particles emit+1 .. emit+99 move to the
     sheet, the rest keep their state; C's truncating integer division and remainder of the
