@@ -34,8 +34,8 @@ UNIT = "particle-steps/s"
 L2_FLUSH_BYTES = 512 << 20
 
 # Algorithmic bytes per particle per launch of each stage of the fused LINEAR_GRID step
-# (each array counted once per stage; neighbour re-reads and the per-brick cell-table reads
-# are not counted). Stated with their derivation in the design doc.
+# (each array counted once per stage; neighbour re-reads, neighbour lists and the per-brick
+# cell-table reads are not counted); the comment beside each entry is its derivation.
 STAGE_BYTES_PER_PARTICLE = {
     "front_end": 16 + 4 + 4,          # R pos, W key, R previous sorted key (sparse table clear)
     "sort": 12 + 16 + 80,             # pass0 R key W key,val; pass1 R/W key,val; pass2 + gather pos,vel
