@@ -48,18 +48,6 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
     return m;
 }
 
-// Adds 1 to the shared-memory histogram bin s_h[bin] for the calling lane. The lanes that
-// arrive together add once between them when they all name the same bin (consecutive
-// particles share their keys' high digits, and 32 same-address atomics would serialise).
-__device__ __forceinline__ void hist_add(uint32_t* s_h, uint32_t bin) {
-    const uint32_t mask = __activemask();
-    if (__reduce_min_sync(mask, bin) == __reduce_max_sync(mask, bin)) {
-        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(mask) - 1)) atomicAdd(&s_h[bin], (uint32_t)__popc(mask));
-    } else {
-        atomicAdd(&s_h[bin], 1u);
-    }
-}
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }

@@ -95,7 +95,7 @@ __global__ void k2_advance_hash(P2* __restrict__ st, float2* __restrict__ prev, 
         for (int q = 0; q < passes; ++q) {
             const int shift = q * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, end_bit - shift);
-            hist_add(s_h, q * SORT_RADIX + ((key >> shift) & ((1u << bits) - 1u)));
+            atomicAdd(&s_h[q * SORT_RADIX + ((key >> shift) & ((1u << bits) - 1u))], 1u);
         }
     }
     __syncthreads();

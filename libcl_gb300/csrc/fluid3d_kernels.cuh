@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos, KP
         for (int p = 0; p < passes; ++p) {
             const int shift = p * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
-            hist_add(s_h, p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u)));
+            atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
         }
         if (CLEAR) {
             const uint32_t pk = prev_keys[i];
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ p
         for (int q = 0; q < passes; ++q) {
             const int shift = q * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
-            hist_add(s_h, q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u)));
+            atomicAdd(&s_h[q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
         }
         if (CLEAR) {
             const uint32_t pk = prev_keys[i];

@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ 
         for (int p = 0; p < passes; ++p) {
             const int shift = start_bit + p * SORT_RADIX_BITS;
             const int bits = min(SORT_RADIX_BITS, end_bit - shift);
-            hist_add(s_h, p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u)));
+            atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
         }
     }
     __syncthreads();
