@@ -68,6 +68,8 @@ struct gbsph_fluid3d_s {
     uint16_t* nbr = nullptr;      // per particle NBR_CAP neighbour slots (density -> forces)
     uint64_t* nbr_meta = nullptr;  // per particle: sub-list lengths, scan flag (bit 63)
     uint32_t* hash_tables = nullptr;  // cell start / end, REF_BUCKETS each
+    uint32_t* xlist = nullptr;        // REFERENCE_HASH fused step: XL_CAP neighbours + count per particle
+    size_t xlist_n = 0;
     uint2* table = nullptr;           // LINEAR_GRID interleaved table
     size_t table_cells = 0;
     bool table_clean = false;  // table empty except the runs of keys_c
@@ -273,9 +275,19 @@ int ensure_tables(H* h) {
             h->table_clean = false;
             invalidate_graph(h);
         }
-    } else if (!h->hash_tables) {
-        GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->hash_tables, 2 * (size_t)REF_BUCKETS * 4));
-        GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->hash_tables, 0xFF, 2 * (size_t)REF_BUCKETS * 4));
+    } else {
+        if (!h->hash_tables) {
+            GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->hash_tables, 2 * (size_t)REF_BUCKETS * 4));
+            GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->hash_tables, 0xFF, 2 * (size_t)REF_BUCKETS * 4));
+        }
+        if (h->xlist_n != h->n_alloc) {  // the fused step's neighbour lists
+            if (h->xlist) cudaFree(h->xlist);
+            h->xlist = nullptr;
+            h->xlist_n = 0;
+            GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->xlist, std::max<size_t>(h->n_alloc, 1) * (XL_CAP + 1) * 4));
+            h->xlist_n = h->n_alloc;
+            invalidate_graph(h);
+        }
     }
     return GBSPH_OK;
 }
@@ -344,23 +356,38 @@ int st_bounds(H* h, const KParams& kp, cudaStream_t s, bool full_clear) {
     return GBSPH_OK;
 }
 
-int st_density_exact(H* h, const KParams& kp, cudaStream_t s) {
+// Exact (reference-order) density and forces. With lists (the fused REFERENCE_HASH step, where
+// the two run back to back on the same sorted state) the density kernel records each
+// particle's in-range neighbours and the force kernel walks them instead of the buckets.
+int st_density_exact(H* h, const KParams& kp, cudaStream_t s, bool lists = false) {
+    uint32_t* xl = h->xlist;
+    uint32_t* xc = h->xlist ? h->xlist + (size_t)h->xlist_n * XL_CAP : nullptr;
     if (kp.key_mode == GBSPH_KEY_LINEAR_GRID)
-        k_density_exact<GBSPH_KEY_LINEAR_GRID><<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, PairTable{h->table}, kp);
+        k_density_exact<GBSPH_KEY_LINEAR_GRID, PairTable, false><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, PairTable{h->table}, kp, nullptr, nullptr);
+    else if (lists && xl)
+        k_density_exact<GBSPH_KEY_REFERENCE_HASH, SplitTable, true><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp, xl, xc);
     else
-        k_density_exact<GBSPH_KEY_REFERENCE_HASH><<<grid1(kp.n), 256, 0, s>>>(
-            h->spos, h->svel, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp);
+        k_density_exact<GBSPH_KEY_REFERENCE_HASH, SplitTable, false><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp, nullptr, nullptr);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
 
-int st_forces_exact(H* h, const KParams& kp, cudaStream_t s) {
+int st_forces_exact(H* h, const KParams& kp, cudaStream_t s, bool lists = false) {
+    const uint32_t* xl = h->xlist;
+    const uint32_t* xc = h->xlist ? h->xlist + (size_t)h->xlist_n * XL_CAP : nullptr;
     if (kp.key_mode == GBSPH_KEY_LINEAR_GRID)
-        k_forces_exact<GBSPH_KEY_LINEAR_GRID><<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, P4(h, 2), h->index,
-                                                                           PairTable{h->table}, kp);
+        k_forces_exact<GBSPH_KEY_LINEAR_GRID, PairTable, false><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, P4(h, 2), h->index, PairTable{h->table}, kp, nullptr, nullptr);
+    else if (lists && xl)
+        k_forces_exact<GBSPH_KEY_REFERENCE_HASH, SplitTable, true><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, P4(h, 2), h->index, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp, xl, xc);
     else
-        k_forces_exact<GBSPH_KEY_REFERENCE_HASH><<<grid1(kp.n), 256, 0, s>>>(
-            h->spos, h->svel, P4(h, 2), h->index, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp);
+        k_forces_exact<GBSPH_KEY_REFERENCE_HASH, SplitTable, false><<<grid1(kp.n), 256, 0, s>>>(
+            h->spos, h->svel, P4(h, 2), h->index, SplitTable{h->hash_tables, h->hash_tables + REF_BUCKETS}, kp,
+            nullptr, nullptr);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
@@ -485,10 +512,10 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
     } else {
         RC(st_bounds(h, kp, s, true));
         RC(mark(h, 3, s));
-        RC(st_density_exact(h, kp, s));
+        RC(st_density_exact(h, kp, s, true));
         RC(mark(h, 4, s));
         if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
-        RC(st_forces_exact(h, kp, s));
+        RC(st_forces_exact(h, kp, s, true));
         if (!h->hook) {
             k_post_fused<<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2), kp);
             GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
@@ -621,6 +648,7 @@ GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h) {
         if (b.owned && b.ptr) cudaFree(b.ptr);
     free_particle_arrays(h);
     if (h->hash_tables) cudaFree(h->hash_tables);
+    if (h->xlist) cudaFree(h->xlist);
     if (h->table) cudaFree(h->table);
     if (h->err) cudaFree(h->err);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);

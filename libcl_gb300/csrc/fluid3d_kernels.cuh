@@ -308,15 +308,23 @@ __device__ __forceinline__ float exact_len(float vx, float vy, float vz) {
     return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz)));
 }
 
-// clCalculateDensity, libCL/phys/oclFluid3D.cl:150-200.
-template <int MODE, class Table>
+// In-range neighbours the exact density kernel records per particle for the exact force
+// kernel (sorted indices in visiting order); a particle with more is scanned again.
+constexpr uint32_t XL_CAP = 64;
+
+// clCalculateDensity, libCL/phys/oclFluid3D.cl:150-200. With RECORD, the in-range neighbours
+// j (visiting order, repeats of a bucket visited twice included) go to xl[particle][.] and
+// their number to xc[particle].
+template <int MODE, class Table, bool RECORD>
 __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos, float4* __restrict__ svel,
-                                                       Table tab, KParams kp) {
+                                                       Table tab, KParams kp, uint32_t* __restrict__ xl,
+                                                       uint32_t* __restrict__ xc) {
     const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
     if (particle >= kp.n) return;
     const float4 posI = spos[particle];
     float density = 0.0f;
     int count = 0;
+    uint32_t* mine = RECORD ? xl + (size_t)particle * XL_CAP : nullptr;
     for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
         for (uint32_t j = start; j < end; j++) {
             if (j == particle) continue;
@@ -325,10 +333,12 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
             if (vlen < kp.h) {
                 const float t = __fsub_rn(__fmul_rn(kp.h, kp.h), __fmul_rn(vlen, vlen));
                 density = __fadd_rn(density, __fmul_rn(__fmul_rn(t, t), t));
+                if (RECORD && (uint32_t)count < XL_CAP) mine[count] = j;
                 count++;
             }
         }
     });
+    if (RECORD) xc[particle] = (uint32_t)count;
     // The reference writes .w in place while other work-items read .xyz only; here every
     // thread has read all it needs before any write lands on a different particle, because
     // the writes only touch .w which no thread of this kernel reads.
@@ -344,36 +354,48 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
 }
 
 // clCalculateForces, libCL/phys/oclFluid3D.cl:202-255: force[index[i]] += SPH force, w = 0.
-template <int MODE, class Table>
+// With LISTED, a particle whose in-range neighbours the density kernel recorded (xc <= XL_CAP)
+// takes them from its list, in the same visiting order, instead of scanning the buckets again:
+// the same pairs in the same order, so the same sums, but the warp's threads step through
+// their pairs together rather than each meeting its in-range candidates at different steps.
+template <int MODE, class Table, bool LISTED>
 __global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__ spos,
                                                       const float4* __restrict__ svel,
                                                       float4* __restrict__ force,
                                                       const uint32_t* __restrict__ index,
-                                                      Table tab, KParams kp) {
+                                                      Table tab, KParams kp, const uint32_t* __restrict__ xl,
+                                                      const uint32_t* __restrict__ xc) {
     const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
     if (particle >= kp.n) return;
     const float4 posI = spos[particle], velI = svel[particle];
     float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-    for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
-        for (uint32_t j = start; j < end; j++) {
-            if (j == particle) continue;
-            const float4 posJ = spos[j];
-            const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
-            const float vlen = exact_len(vx, vy, vz);
-            if (vlen < kp.h) {
-                const float4 velJ = svel[j];
-                const float density2 = __fmul_rn(posI.w, posJ.w);
-                const float s = __fdiv_rn(__fadd_rn(velI.w, velJ.w), density2);
-                const float hr = __fsub_rn(kp.h, vlen);
-                px = __fadd_rn(px, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vx, vlen), hr), hr)));
-                py = __fadd_rn(py, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vy, vlen), hr), hr)));
-                pz = __fadd_rn(pz, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vz, vlen), hr), hr)));
-                qx = __fadd_rn(qx, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.x, velI.x), density2), hr));
-                qy = __fadd_rn(qy, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.y, velI.y), density2), hr));
-                qz = __fadd_rn(qz, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.z, velI.z), density2), hr));
-            }
+    auto pair = [&](uint32_t j) {
+        const float4 posJ = spos[j];
+        const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
+        const float vlen = exact_len(vx, vy, vz);
+        if (vlen < kp.h) {
+            const float4 velJ = svel[j];
+            const float density2 = __fmul_rn(posI.w, posJ.w);
+            const float s = __fdiv_rn(__fadd_rn(velI.w, velJ.w), density2);
+            const float hr = __fsub_rn(kp.h, vlen);
+            px = __fadd_rn(px, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vx, vlen), hr), hr)));
+            py = __fadd_rn(py, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vy, vlen), hr), hr)));
+            pz = __fadd_rn(pz, __fmul_rn(s, __fmul_rn(__fmul_rn(__fdiv_rn(vz, vlen), hr), hr)));
+            qx = __fadd_rn(qx, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.x, velI.x), density2), hr));
+            qy = __fadd_rn(qy, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.y, velI.y), density2), hr));
+            qz = __fadd_rn(qz, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.z, velI.z), density2), hr));
         }
-    });
+    };
+    const uint32_t nl = LISTED ? xc[particle] : EMPTY;
+    if (LISTED && nl <= XL_CAP) {
+        const uint32_t* mine = xl + (size_t)particle * XL_CAP;
+        for (uint32_t k = 0; k < nl; ++k) pair(mine[k]);
+    } else {
+        for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
+            for (uint32_t j = start; j < end; j++)
+                if (j != particle) pair(j);
+        });
+    }
     const uint32_t o = index[particle];
     float4 f = force[o];
     f.x = __fadd_rn(f.x, __fmul_rn(__fadd_rn(__fmul_rn(kp.cpress, px), __fmul_rn(kp.cvisc, qx)), kp.mass));

@@ -54,6 +54,25 @@ def test_hash_mode_step_bit_exact(cuda, fused):
     assert f.sync_status() == OK
 
 
+def test_hash_mode_fused_lists_and_overflow_bit_exact(cuda):
+    """REFERENCE_HASH fused step on a block at 0.7 x the default spacing: about three quarters
+    of the particles have more in-range neighbours than the force kernel's recorded lists hold
+    (they scan the buckets again), the rest walk their lists; all bit-exact."""
+    sc = hash_block(22)
+    sp = sc.params.spacing
+    sc.pos = lattice(22, 22, 22, 0.7 * sp, (-7.7 * sp,) * 3, 0.1 * sp, 14)
+    vel = perturbed(sc)
+    f = make_fluid(sc, fused=True, vel=vel)
+    f.compute()
+    g, gs = sorted_outputs(f, REF_BUCKETS), state(f)
+    r, rs = oracle_step(sc, vel, ref_sort=True)
+    assert_bit_exact(g["spos"], r.spos, "sorted position (.w = density)")
+    assert_bit_exact(g["svel"], r.svel, "sorted velocity (.w = pressure)")
+    for k in ("pos", "vel", "force"):
+        assert_bit_exact(gs[k], rs[k], k)
+    assert f.sync_status() == OK
+
+
 def test_linear_staged_step_bit_exact(cuda):
     sc = block_collapse_3d(32, 16, 32)
     vel = perturbed(sc)
