@@ -35,7 +35,8 @@ float bits_to_float(uint32_t b) {
 // Smallest float x >= 0 with sqrtf(x) >= h. sqrtf is correctly rounded and monotone, so for
 // every float r2 >= 0: (sqrtf(r2) < h) == (r2 < threshold).
 float r2_threshold(float h) {
-    if (!(h > 0.0f) || std::isinf(h)) return 0.0f;
+    if (!(h > 0.0f)) return 0.0f;  // nothing is nearer than h
+    if (std::isinf(h)) return h;   // every finite distance is
     uint32_t lo = 0, hi = 0x7f800000u;  // sqrtf(+0) = 0 < h, sqrtf(inf) = inf >= h
     while (hi - lo > 1) {
         const uint32_t mid = lo + (hi - lo) / 2;

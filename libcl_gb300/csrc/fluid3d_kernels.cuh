@@ -303,9 +303,12 @@ __device__ __forceinline__ void for_each_neighbour_cell(const KParams& kp, const
             }
 }
 
-// fast_length of (a - b) with w = 0, evaluated as ((x*x + y*y) + z*z), correctly rounded sqrt.
-__device__ __forceinline__ float exact_len(float vx, float vy, float vz) {
-    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz)));
+// fast_length of (a - b) with w = 0 is the correctly rounded sqrt of exact_r2 =
+// ((x*x + y*y) + z*z). The correctly rounded sqrt is monotone, so sqrt(r2) < h exactly when
+// r2 < kp.r2_thresh (the least float whose sqrt is >= h): the kernels test r2 and take the
+// root of in-range candidates only.
+__device__ __forceinline__ float exact_r2(float vx, float vy, float vz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(vx, vx), __fmul_rn(vy, vy)), __fmul_rn(vz, vz));
 }
 
 // In-range neighbours the exact density kernel records per particle for the exact force
@@ -329,8 +332,9 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
         for (uint32_t j = start; j < end; j++) {
             if (j == particle) continue;
             const float4 pj = spos[j];
-            const float vlen = exact_len(__fsub_rn(posI.x, pj.x), __fsub_rn(posI.y, pj.y), __fsub_rn(posI.z, pj.z));
-            if (vlen < kp.h) {
+            const float r2 = exact_r2(__fsub_rn(posI.x, pj.x), __fsub_rn(posI.y, pj.y), __fsub_rn(posI.z, pj.z));
+            if (r2 < kp.r2_thresh) {  // fast_length < h
+                const float vlen = __fsqrt_rn(r2);
                 const float t = __fsub_rn(__fmul_rn(kp.h, kp.h), __fmul_rn(vlen, vlen));
                 density = __fadd_rn(density, __fmul_rn(__fmul_rn(t, t), t));
                 if (RECORD && (uint32_t)count < XL_CAP) mine[count] = j;
@@ -372,8 +376,9 @@ __global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__
     auto pair = [&](uint32_t j) {
         const float4 posJ = spos[j];
         const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
-        const float vlen = exact_len(vx, vy, vz);
-        if (vlen < kp.h) {
+        const float r2 = exact_r2(vx, vy, vz);
+        if (r2 < kp.r2_thresh) {  // fast_length < h
+            const float vlen = __fsqrt_rn(r2);
             const float4 velJ = svel[j];
             const float density2 = __fmul_rn(posI.w, posJ.w);
             const float s = __fdiv_rn(__fadd_rn(velI.w, velJ.w), density2);
