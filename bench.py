@@ -354,6 +354,31 @@ def extra_2d(stream, steps: int = 500) -> dict:
     return out
 
 
+def extra_hash_mode(stream, steps: int = 50) -> dict:
+    """The 1M 3D block collapse on the reference's default keys (262,144-bucket hash, the exact
+    kernels in the reference's summation order), from the start of the collapse."""
+    import statistics
+    from libcl_gb300 import KEY_REFERENCE_HASH, OPT_PROFILE, Fluid3D
+    from libcl_gb300.scenes import block_collapse_3d
+    sc = block_collapse_3d()
+    f = Fluid3D()
+    load_scene(f, sc)
+    f.getParameters().keyMode = KEY_REFERENCE_HASH
+    for _ in range(5):
+        f.compute(stream)
+    t = _time_steps(lambda: f.compute(stream), steps, stream)
+    f.set_option(OPT_PROFILE, 1)
+    acc = {}
+    for _ in range(5):
+        f.compute(stream)
+        for k, v in f.stage_times().items():
+            acc.setdefault(k, []).append(v)
+    f.set_option(OPT_PROFILE, 0)
+    assert f.sync_status() == 0
+    return {"particles": sc.n, "ms_per_step": t / steps, "particle_steps_per_s": sc.n * steps / (t * 1e-3),
+            "stages_ms": {k: statistics.median(v) for k, v in acc.items()}}
+
+
 def extra_adjoint(stream) -> dict:
     """Forward + adjoint against forward alone: the differentiable rollout (65,536 particles,
     200 steps, checkpoint every 20) and the 1M block collapse (20 steps, checkpoint every 10).
@@ -764,6 +789,7 @@ def main(argv=None) -> int:
             del fluid, flush
             torch.cuda.empty_cache()
             result["extras"] = {"batched_256_scenes": extra_batched(stream), "sort_16m": extra_sort(stream),
+                                "reference_hash_keys_1m": extra_hash_mode(stream),
                                 "two_d": extra_2d(stream), "adjoint": extra_adjoint(stream),
                                 "bvh_1m_triangles": extra_bvh(stream),
                                 "bvh_lines_1m_segments": extra_bvh_lines(stream)}
