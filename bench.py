@@ -645,6 +645,9 @@ def main(argv=None) -> int:
     ap.add_argument("--quick", action="store_true", help="skip e2e/profile/baseline legs (for ncu)")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / sort / 2D side measurements")
     ap.add_argument("--brick-width", type=int, default=0, help="cells per neighbour brick (0: library default)")
+    ap.add_argument("--keys", default="linear", choices=["linear", "reference-hash"],
+                    help="cell keys of the timed step: the bounded linear grid (default) or the reference's "
+                         "262,144-bucket hash with the exact kernels")
     ap.add_argument("--profile-suite", action="store_true",
                     help="run every hot path once, untimed (the workload of the per-kernel ncu summary)")
     args = ap.parse_args(argv)
@@ -675,6 +678,9 @@ def main(argv=None) -> int:
     if args.brick_width:
         from libcl_gb300 import OPT_BRICK_WIDTH
         fluid.set_option(OPT_BRICK_WIDTH, args.brick_width)
+    if args.keys == "reference-hash":
+        from libcl_gb300 import KEY_REFERENCE_HASH
+        fluid.getParameters().keyMode = KEY_REFERENCE_HASH
     stream = torch.cuda.current_stream()
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -705,7 +711,9 @@ def main(argv=None) -> int:
         print(f"device status {status}: {fluid.last_error()}", file=sys.stderr)
         return 1
     value = scene.n * args.steps * world / (t_ms * 1e-3)
-    launches_per_step = 7  # hash, 3 sort passes, bounds, density, forces
+    # linear grid: hash, 3 sort passes, bounds, density, forces; reference hash: the same with
+    # the exact density and forces, plus the fused clip-box / integration kernel
+    launches_per_step = 7 if args.keys == "linear" else 8
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -714,7 +722,8 @@ def main(argv=None) -> int:
         "data": "synthetic (seeded jittered lattice, block_collapse_3d seed 2)",
         "config": {"workload": "3d_block_collapse_1M", "particles": scene.n, "lattice": [128, 64, 128],
                    "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed steps (512 MiB write)", "graph": True},
+                   "l2": "flushed between timed steps (512 MiB write)", "graph": True,
+                   "keys": args.keys},
         "gpu_launches": launches_per_step * args.steps,
         "step_ms_p50": statistics.median(step_ms),
     }
@@ -743,22 +752,23 @@ def main(argv=None) -> int:
         dom = max(stage_ms, key=stage_ms.get)
         dom_bytes = STAGE_BYTES_PER_PARTICLE[dom] * scene.n
         ach = stage_gbs[dom]
-        traffic = None
-        tp = ROOT / "profiles" / "traffic.json"
-        if tp.exists():
-            traffic = json.loads(tp.read_text()).get(dom)
-        result["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
-                              "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
-                              "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": stage_ms[dom]}
-        fl = neighbour_flops(fluid, scene.params)
-        fp32_peak = sm_count(torch) * 128 * 2 * (result["clocks"].get("sm_mhz") or 2070.0) * 1e6 / 1e12
-        fl["fp32_peak_tflops"] = fp32_peak
-        fl["fp32_peak_source"] = "derived: SMs x 128 FP32 lanes x 2 (FMA) x median SM clock of the timed run"
-        for stg in ("density", "forces"):
-            tf = fl[f"{stg}_flops_per_particle"] * scene.n / (stage_ms[stg] * 1e-3) / 1e12
-            fl[f"{stg}_achieved_tflops"] = tf
-            fl[f"{stg}_fp32_frac"] = tf / fp32_peak
-        result["flops"] = fl
+        if args.keys == "linear":  # byte and flop counts of the linear-grid step's kernels
+            traffic = None
+            tp = ROOT / "profiles" / "traffic.json"
+            if tp.exists():
+                traffic = json.loads(tp.read_text()).get(dom)
+            result["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                                  "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
+                                  "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": stage_ms[dom]}
+            fl = neighbour_flops(fluid, scene.params)
+            fp32_peak = sm_count(torch) * 128 * 2 * (result["clocks"].get("sm_mhz") or 2070.0) * 1e6 / 1e12
+            fl["fp32_peak_tflops"] = fp32_peak
+            fl["fp32_peak_source"] = "derived: SMs x 128 FP32 lanes x 2 (FMA) x median SM clock of the timed run"
+            for stg in ("density", "forces"):
+                tf = fl[f"{stg}_flops_per_particle"] * scene.n / (stage_ms[stg] * 1e-3) / 1e12
+                fl[f"{stg}_achieved_tflops"] = tf
+                fl[f"{stg}_fp32_frac"] = tf / fp32_peak
+            result["flops"] = fl
         step_bytes = sum(STAGE_BYTES_PER_PARTICLE.values()) * scene.n + 8 * n_cells_occ
         result["stages"] = {"ms": stage_ms, "gbs": stage_gbs, "occupied_cells": n_cells_occ,
                             "step_algorithmic_bytes": step_bytes,
