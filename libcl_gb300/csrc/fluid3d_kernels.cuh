@@ -316,8 +316,9 @@ __device__ __forceinline__ float exact_r2(float vx, float vy, float vz) {
 constexpr uint32_t XL_CAP = 64;
 
 // clCalculateDensity, libCL/phys/oclFluid3D.cl:150-200. With RECORD, the in-range neighbours
-// j (visiting order, repeats of a bucket visited twice included) go to xl[particle][.] and
-// their number to xc[particle].
+// j (visiting order, repeats of a bucket visited twice included) go to xl[k * n + particle]
+// (entry-major, so that the force kernel's threads, stepping through their lists together,
+// read consecutive words) and their number to xc[particle].
 template <int MODE, class Table, bool RECORD>
 __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos, float4* __restrict__ svel,
                                                        Table tab, KParams kp, uint32_t* __restrict__ xl,
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
     const float4 posI = spos[particle];
     float density = 0.0f;
     int count = 0;
-    uint32_t* mine = RECORD ? xl + (size_t)particle * XL_CAP : nullptr;
+    uint32_t* mine = RECORD ? xl + particle : nullptr;
     for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
         for (uint32_t j = start; j < end; j++) {
             if (j == particle) continue;
@@ -337,7 +338,7 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
                 const float vlen = __fsqrt_rn(r2);
                 const float t = __fsub_rn(__fmul_rn(kp.h, kp.h), __fmul_rn(vlen, vlen));
                 density = __fadd_rn(density, __fmul_rn(__fmul_rn(t, t), t));
-                if (RECORD && (uint32_t)count < XL_CAP) mine[count] = j;
+                if (RECORD && (uint32_t)count < XL_CAP) mine[(size_t)count * kp.n] = j;
                 count++;
             }
         }
@@ -393,8 +394,7 @@ __global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__
     };
     const uint32_t nl = LISTED ? xc[particle] : EMPTY;
     if (LISTED && nl <= XL_CAP) {
-        const uint32_t* mine = xl + (size_t)particle * XL_CAP;
-        for (uint32_t k = 0; k < nl; ++k) pair(mine[k]);
+        for (uint32_t k = 0; k < nl; ++k) pair(xl[(size_t)k * kp.n + particle]);
     } else {
         for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
             for (uint32_t j = start; j < end; j++)
