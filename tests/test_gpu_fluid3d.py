@@ -73,6 +73,22 @@ def test_hash_mode_fused_lists_and_overflow_bit_exact(cuda):
     assert f.sync_status() == OK
 
 
+def test_hash_mode_fused_equals_staged_over_steps(cuda):
+    """The fused REFERENCE_HASH step (recorded neighbour lists) against the staged stages
+    (the force kernel scanning the buckets): bitwise equal state after each of 6 steps."""
+    sc = hash_block(24)
+    vel = perturbed(sc, sigma=0.2)
+    a = make_fluid(sc, fused=True, vel=vel)
+    b = make_fluid(sc, fused=False, vel=vel)
+    for step in range(6):
+        a.compute()
+        b.compute()
+        sa, sb = state(a), state(b)
+        for k in sa:
+            assert_bit_exact(sa[k], sb[k], f"{k} after step {step + 1}")
+    assert a.sync_status() == OK and b.sync_status() == OK
+
+
 def test_linear_staged_step_bit_exact(cuda):
     sc = block_collapse_3d(32, 16, 32)
     vel = perturbed(sc)
