@@ -975,12 +975,14 @@ __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& v
     acc[5] = fmaf(vj.z - vi.z, cv, acc[5]);
 }
 
-// Forces (pressure + viscosity) for every particle of the occupied bricks. The brick's rows
-// are staged exactly as in k_density_brick; each lane takes one target and evaluates the
-// in-range pairs that the density kernel recorded in the target's sub-lists. Targets whose lists are unusable
-// (overflow, unstaged brick) are handled by scanning the rows. With FUSED the clip-box,
-// integrate-force, gravity and integrate-velocity stages follow in registers; otherwise the
-// SPH force is added to force[index[i]] (with w = 0) as clCalculateForces does.
+// Forces (pressure + viscosity) for every particle of the occupied bricks
+// (clCalculateForces, libCL/phys/oclFluid3D.cl:202-255). The brick's rows are staged exactly
+// as in k_density_brick; two lanes take a target and evaluate the in-range pairs that the
+// density kernel recorded in the target's sub-lists. A target whose sub-lists overflowed is
+// scanned over its rows by its whole warp after the list walk; in an unstaged brick both lanes
+// scan the rows in global memory. With FUSED the clip-box, integrate-force, gravity and
+// integrate-velocity stages follow in registers; otherwise the SPH force is added to
+// force[index[i]] (with w = 0) as clCalculateForces does.
 template <int DIMS, bool FUSED, bool BATCH>
 __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* __restrict__ spos,
                                                                const float4* __restrict__ svel,
