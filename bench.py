@@ -494,13 +494,14 @@ def extra_bvh_lines(stream) -> dict:
 
 def profile_suite(stream) -> None:
     """One untimed pass over every hot path, sized for a per-kernel ncu capture (about 1 GB on
-    the device at a time): 3 fused steps of the 1M block collapse; the 16M uniform and Morton
+    the device at a time): 3 fused steps of the 1M block collapse, on the linear grid and on the
+    reference's hash keys (exact kernels); the 16M uniform and Morton
     sorts with cell bounds; 2 steps of a 32-scene batch; a 10-step adjoint (checkpoint every
     5) of the 65,536-particle block; the 1M-triangle and 1M-segment BVH builds and a collision
     pass; 3 steps of the 2D dam break (dims = 2) and of the 2D relaxation model."""
     import torch
-    from libcl_gb300 import (BUF_FORCE, BUF_POSITION, BUF_VELOCITY, Adjoint3D, Batch3D, BvhLines, BvhTrimesh,
-                             Fluid2D, Fluid3D, RadixSort, default_params)
+    from libcl_gb300 import (BUF_FORCE, BUF_POSITION, BUF_VELOCITY, KEY_REFERENCE_HASH, Adjoint3D, Batch3D,
+                             BvhLines, BvhTrimesh, Fluid2D, Fluid3D, RadixSort, default_params)
     from libcl_gb300.scenes import (SplitMix64, batched_ensemble, block_collapse_3d, dam_break_2d,
                                     differentiable_block, lattice_soup, segment_lattice, sphere_mesh)
 
@@ -508,13 +509,16 @@ def profile_suite(stream) -> None:
         torch.cuda.synchronize()
         torch.cuda.empty_cache()
 
-    f = Fluid3D()
-    load_scene(f, block_collapse_3d())
-    for _ in range(3):
-        f.compute(stream)
-    assert f.sync_status() == 0
-    del f
-    done()
+    for hash_keys in (False, True):
+        f = Fluid3D()
+        load_scene(f, block_collapse_3d())
+        if hash_keys:
+            f.getParameters().keyMode = KEY_REFERENCE_HASH
+        for _ in range(3):
+            f.compute(stream)
+        assert f.sync_status() == 0
+        del f
+        done()
     n = 1 << 24
     rng = SplitMix64(3)
     keys = torch.from_numpy((rng.next_u64(n) >> np.uint64(32)).astype(np.uint32).view(np.int32)).cuda()
