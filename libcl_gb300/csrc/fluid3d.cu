@@ -606,10 +606,14 @@ GBSPH_API int gbsph_fluid3d_params_derive(gbsph_fluid3d_params* p) {
         p->pressureConstant = (float)(30.0 / (pi * std::pow(h, 5.0)));
         p->viscosityConstant = (float)((double)p->viscosity * 40.0 / (pi * std::pow(h, 5.0)));
     } else {
-        // DensityConstant / PressureConstant / ViscosityConstant, libCL/phys/oclFluid3D.cl:123-128
+        // DensityConstant / PressureConstant / ViscosityConstant, libCL/phys/oclFluid3D.cl:123-128,
+        // with OpenCL C's types: M_PI_F is a float, so 64.0*M_PI_F*pow(h, 9) is a double
+        // product while M_PI_F * pow(h, 6.0f) is a float product, divided into -45.0 in double.
+        const float pi_f = (float)M_PI;
         p->kernelConstant = (float)(315.0 / (64.0 * pi * (double)std::pow(p->cellSize, 9.0f)));
-        p->viscosityConstant = (float)(-(double)p->viscosity * (-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
-        p->pressureConstant = (float)(-(-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
+        p->viscosityConstant =
+            (float)(-(double)p->viscosity * (-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
+        p->pressureConstant = (float)(-(-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
     }
     return GBSPH_OK;
 }

@@ -494,15 +494,18 @@ static __global__ void k_integrate_velocity(float4* __restrict__ pos, const floa
 
 // clEmitter (libCL/phys/oclFluid3D.cl:273-282): particles emit+1 .. emit+99 are placed on a
 // 10-wide sheet at y = 0.6 (index = emit - particle, negative, with C's truncating / and %)
-// and given velocity (0, emit_speed, 0). The literal 0.6 is taken as a float.
+// and given velocity (0, emit_speed, 0). The z lane `0.6 + index%10*2*radius` adds the float
+// product to the double literal 0.6 in double and rounds the sum to float once (OpenCL C on a
+// device with doubles, as the reference's kernels compile on the host and GPU OpenCL stacks).
 static __global__ void k_emitter(float4* __restrict__ pos, float4* __restrict__ vel, uint32_t n, uint32_t emit,
                                  float emit_speed, float radius) {
     const uint32_t particle = blockIdx.x * blockDim.x + threadIdx.x;
     if (particle >= n) return;
     if (particle > emit && particle < emit + 100u) {
         const int index = (int)(emit - particle);
+        const float dz = __fmul_rn((float)(index % 10 * 2), radius);
         pos[particle] = make_float4(__fmul_rn((float)(index / 10 * 2), radius), 0.6f,
-                                    __fadd_rn(0.6f, __fmul_rn((float)(index % 10 * 2), radius)), 1.0f);
+                                    __double2float_rn(__dadd_rn(0.6, (double)dz)), 1.0f);
         vel[particle] = make_float4(0.0f, emit_speed, 0.0f, 1.0f);
     }
 }

@@ -282,10 +282,12 @@ void orc_init_fluid_params(gbsph_fluid3d_params* p) {
     p->spacing = (float)(0.87 * (double)std::pow(p->mass / p->density, 1 / 3.0f));
     p->particleRadius = (float)(0.5 * (double)p->spacing);
     p->cellSize = (float)(2.0 * (double)p->spacing);
-    const double pi = (double)(float)M_PI;  // M_PI_F
-    p->kernelConstant = (float)(315.0 / (64.0 * pi * (double)std::pow(p->cellSize, 9.0f)));
-    p->viscosityConstant = (float)(-(double)p->viscosity * (-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
-    p->pressureConstant = (float)(-(-45.0 / (pi * (double)std::pow(p->cellSize, 6.0f))));
+    // M_PI_F is a float: 64.0*M_PI_F is a double product, but M_PI_F * pow(h, 6.0f) (the
+    // pressure and viscosity constants) is a float product, divided into -45.0 in double.
+    const float pi_f = 3.14159274101257f;  // M_PI_F
+    p->kernelConstant = (float)(315.0 / (64.0 * (double)pi_f * (double)std::pow(p->cellSize, 9.0f)));
+    p->viscosityConstant = (float)(-(double)p->viscosity * (-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
+    p->pressureConstant = (float)(-(-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
     p->gravity[0] = -9.8f * 0.0f;
     p->gravity[1] = -9.8f * 0.0f;
     p->gravity[2] = -9.8f * 1.0f;

@@ -93,3 +93,18 @@ def perturbed(scene: Scene3D, seed: int = 5, sigma: float = 0.05) -> np.ndarray:
 
 __all__ = ["hash_block", "make_fluid", "state", "sorted_outputs", "rel_err", "pos_err", "RTOL", "set_params",
            "clone_params", "perturbed"]
+
+
+def emitter_expected(pos: np.ndarray, vel: np.ndarray, emit: int, speed: float, radius: float):
+    """The state clEmitter (libCL/phys/oclFluid3D.cl:273-282) leaves: particles emit+1 ..
+    emit+99 go to a 10-wide sheet at y = 0.6 with velocity (0, speed, 0, 1). index = emit -
+    particle is negative; / and % truncate as in C. The z lane adds the float product
+    index%10*2*radius to the double literal 0.6 in double, then rounds to float."""
+    pos, vel = pos.copy(), vel.copy()
+    r = np.float32(radius)
+    for p in range(emit + 1, min(emit + 100, pos.shape[0])):
+        index = emit - p
+        q, m = int(index / 10), int(np.fmod(index, 10))
+        pos[p] = [np.float32(q * 2) * r, 0.6, np.float32(0.6 + np.float64(np.float32(m * 2) * r)), 1.0]
+        vel[p] = [0.0, speed, 0.0, 1.0]
+    return pos.astype(np.float32), vel.astype(np.float32)

@@ -25,3 +25,14 @@ def block_state(nx: int = 128, ny: int = 128, spacing: float = 0.06, origin=(1.0
     st[:, 1] = origin[1] + iy.ravel() * spacing + (rng.uniform(n) - 0.5) * 0.1 * spacing
     st[:, 4] = 0.7
     return st
+
+
+def emitter2d_expected(state: np.ndarray, emit: int, particle_size: float) -> np.ndarray:
+    """The state clEmitter (libCL/phys/oclFluid2D.cl:342-352) leaves: only particle emit+1
+    moves, to (1, 14 + (p%4)*12*particleSize) with velocity (25, 1) and age 1."""
+    want = state.copy()
+    p = emit + 1
+    if p < state.shape[0]:
+        want[p, :4] = [1.0, np.float32(14.0) + np.float32(p % 4 * 12) * np.float32(particle_size), 25.0, 1.0]
+        want[p, 5] = 1.0
+    return want

@@ -7,7 +7,7 @@ import pytest
 import oracle
 from libcl_gb300 import (BUF2D_BORDER_STATE, BUF2D_BORDER_VECTOR, BUF2D_CELL, BUF2D_INDEX, BUF2D_PRESSURE,
                          BUF2D_RELAXED, BUF2D_SORTED_STATE, BUF2D_STATE, Fluid2D)
-from scenes2d import block_state, box_mask
+from scenes2d import block_state, box_mask, emitter2d_expected
 
 pytestmark = pytest.mark.gpu
 
@@ -75,8 +75,5 @@ def test_fluid2d_emitter(cuda):
     f.emit(101)
     torch.cuda.synchronize()
     g = f.getStateBuffer().cpu().numpy()
-    want = st.copy()
-    psize = np.float32(f.getParameters().particleSize)
-    want[102, :4] = [1.0, np.float32(14.0) + np.float32(102 % 4 * 12) * psize, 25.0, 1.0]
-    want[102, 5] = 1.0
+    want = emitter2d_expected(st, 101, f.getParameters().particleSize)
     np.testing.assert_array_equal(g.view(np.uint32), want.view(np.uint32))

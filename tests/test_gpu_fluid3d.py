@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 import oracle
-from fluid_helpers import RTOL, hash_block, make_fluid, perturbed, pos_err, rel_err, set_params, sorted_outputs, state
+from fluid_helpers import (RTOL, emitter_expected, hash_block, make_fluid, perturbed, pos_err, rel_err, set_params,
+                           sorted_outputs, state)
 from libcl_gb300 import (ERR_ARGUMENT, ERR_NOT_COMPILED, ERR_SIZE_MISMATCH, OK, OPT_BRICK_WIDTH, REF_BUCKETS,
                          STAGE_GRAVITY, STAGE_INTEGRATE_FORCE, STAGE_INTEGRATE_VELOCITY, Fluid3D)
 from libcl_gb300.scenes import block_collapse_3d, clone_params, lattice, reference_test_scene
@@ -462,21 +463,15 @@ def test_disordered_2d_block_within_tolerance_and_brick_width_free(cuda):
 
 def test_emitter(cuda):
     """clEmitter (libCL/phys/oclFluid3D.cl:273-282): particles emit+1 .. emit+99 move to the
-    sheet, the rest keep their state; C's truncating integer division and remainder of the
-    negative index."""
+    sheet, the rest keep their state (expected values: fluid_helpers.emitter_expected, which
+    the CPU tests pin to the reference's own kernel)."""
     sc = block_collapse_3d(8, 8, 8)
     vel = perturbed(sc)
     f = make_fluid(sc, vel=vel)
     f.emit(200, 1.5)
     g = state(f)
-    r = np.float32(sc.params.particleRadius)
-    pos, v = sc.pos.copy(), vel.copy()
-    for p in range(201, 300):
-        index = 200 - p
-        q, m = int(index / 10), int(np.fmod(index, 10))
-        pos[p] = [np.float32(q * 2) * r, 0.6, np.float32(0.6) + np.float32(m * 2) * r, 1.0]
-        v[p] = [0.0, 1.5, 0.0, 1.0]
-    np.testing.assert_array_equal(g["pos"].view(np.uint32), pos.astype(np.float32).view(np.uint32))
+    pos, v = emitter_expected(sc.pos, vel, 200, 1.5, sc.params.particleRadius)
+    np.testing.assert_array_equal(g["pos"].view(np.uint32), pos.view(np.uint32))
     np.testing.assert_array_equal(g["vel"], v)
 
 
