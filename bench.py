@@ -8,8 +8,10 @@ events on the stream it runs on. Prints one JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the CPU port of the reference's kernels (the oracle; the reference's
-OpenCL kernels cannot run here) on the host cores, on a bounded sample of the same scene.
+--impl reference times the reference's own kernels (libCL/phys/oclFluid3D.cl and
+libCL/sort/oclRadixSort.cl, built for the host cores by oracle/ref/build.py through an OpenCL
+C shim, OpenMP over work-groups) on the same scene, on its own hash keys, without loading
+the product library; where they are not built, the oracle (the CPU port of those kernels).
 With N>1 (torchrun) the plain step does not shard: every rank advances its own replica.
 """
 from __future__ import annotations
@@ -33,16 +35,28 @@ METRIC = "SPH particle-steps/s, 1M 3D block collapse (plain step)"
 UNIT = "particle-steps/s"
 L2_FLUSH_BYTES = 512 << 20
 
-# Algorithmic bytes per particle per launch of each stage of the fused LINEAR_GRID step
-# (each array counted once per stage; neighbour re-reads, neighbour lists and the per-brick
-# cell-table reads are not counted); the comment beside each entry is its derivation.
+# Algorithmic bytes per particle-step of each stage (the fixed per-stage figures of the step's
+# byte budget: each array counted once per stage; neighbour re-reads, neighbour lists and
+# cell-table reads not counted), mapped onto the fused step's launches:
 STAGE_BYTES_PER_PARTICLE = {
-    "front_end": 16 + 4 + 4,          # R pos, W key, R previous sorted key (sparse table clear)
-    "sort": 12 + 16 + 80,             # pass0 R key W key,val; pass1 R/W key,val; pass2 + gather pos,vel
+    "front_end": 16 + 4 + 4,          # hash: R pos 16, W key 4, W index 4
+    "sort": (4 + 16 * 3) + 68,        # histogram R key + 3 x 8-bit passes (R/W key, index), and the
+                                      # reorder fused into the last pass: R index 4, R pos, vel 32,
+                                      # W sorted pos, vel 32
     "bounds": 4,                      # R sorted key (+8 B per occupied cell, added below)
-    "density": 16 + 16 + 4,           # R spos, W spos (w = density), W svel.w
-    "forces": 16 + 16 + 4 + 32 + 32 + 32,  # R spos,svel,index; R/W pos, vel, force
+    "density": 16 + 4,                # R sorted pos 16, W density/pressure 4
+    "forces": 16 + 16 + 4 + 4 + 32,   # R sorted pos, vel, density/pressure, index; W pos, vel
 }
+# The step adds 8 B per cell of the table (its initialisation) and 8 B per occupied cell.
+TABLE_CELLS = 200 * 100 * 200
+# The scene (both arms): the 3D block collapse; `l2` says how the timed steps treat caches.
+WORKLOAD = {"workload": "3d_block_collapse_1M", "particles": 128 * 64 * 128, "lattice": [128, 64, 128],
+            "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5,
+            "l2": "GPU arm: L2 flushed between timed steps (512 MiB write); host arm: not flushed"}
+
+
+def workload_config(world: int) -> dict:
+    return dict(WORKLOAD, parallelism=f"replicas x{world}")
 
 
 def env_rank():
@@ -194,21 +208,76 @@ def load_scene(fluid, scene):
     torch.cuda.synchronize()
 
 
-def cpu_baseline(scene, seconds: float = 10.0):
-    """The oracle (CPU port of the reference kernels, restated 4-bit reference sort) on the
-    full scene, all host threads, for about `seconds` of work."""
+def reference_stepper(prefer_reference: bool = True):
+    """One step of the block collapse as the reference computes it, on the host cores, built
+    without the product library: positions from the seeded lattice (numpy), the System block
+    from clInitFluid's formulas for h = 0.02 and viscosity 0.05, the reference's hash keys
+    (262,144 buckets) and 4-bit block sort, clip box [0,4]x[0,2]x[0,4], gravity argument
+    (0, 9.81f/9.8f, 0). With the reference's kernels built (oracle/ref) they run it
+    (kind "reference"); otherwise, or with prefer_reference False, the oracle does (kind
+    "port"). Returns (step function, kind, threads, particles, description)."""
+    import oracle.ref as ref
+    from libcl_gb300 import Fluid3DParams, KEY_REFERENCE_HASH
+    from libcl_gb300.scenes import lattice
+    h, sp = 0.02, 0.01
+    pos = lattice(128, 64, 128, sp, (0.5 * sp,) * 3, 0.05 * h, 2)
+    vel, force = np.zeros_like(pos), np.zeros_like(pos)
+    use_ref = prefer_reference and ref.available()
+    if use_ref:
+        k = ref.kernel_constants(np.float32(h), np.float32(0.05))
+    else:
+        import oracle
+        k = oracle.kernel_constants(np.float32(h), np.float32(0.05))
+    system = np.array([5e-5, 0.5 * sp, h, 1000.0 * sp ** 3, 0.05, 0.0, 1000.0, sp, 3.0, k[1], k[2], k[0], 500.0],
+                      np.float32)
+    garg = np.array([0.0, np.float32(9.81) / np.float32(9.8), 0.0, 0.0], np.float32)
+    lo, hi = np.zeros(4, np.float32), np.array([4.0, 2.0, 4.0, 0.0], np.float32)
+    if use_ref:
+        threads = ref.set_num_threads(0)
+
+        def step():
+            ref.step3d(pos, vel, force, system, garg, lo, hi)
+        return step, "reference", threads, pos.shape[0], (
+            "the reference's kernels (libCL/phys/oclFluid3D.cl, libCL/sort/oclRadixSort.cl) through an "
+            "OpenCL C shim, work-groups on OpenMP threads, barrier kernels as coroutines")
     import oracle
-    pos, vel, force = scene.pos.copy(), scene.vel.copy(), np.zeros_like(scene.pos)
-    oracle.step(pos, vel, force, scene.params, ref_sort=True)  # warm-up (page-in, thread pool)
+    p = Fluid3DParams()
+    for name, v in zip([f for f, _ in Fluid3DParams._fields_[:13]], system):
+        setattr(p, name, float(v))
+    g = np.float32(-9.8) * garg
+    for i in range(4):
+        p.gravity[i], p.boxMin[i], p.boxMax[i] = float(g[i]), float(lo[i]), float(hi[i])
+    p.keyMode, p.dims = KEY_REFERENCE_HASH, 3
+
+    def step():
+        oracle.step(pos, vel, force, p, ref_sort=True)
+    return step, "port", oracle.num_threads(), pos.shape[0], (
+        "the oracle (the C++ restatement of the reference's kernels, its 4-bit block sort loop-fissioned), "
+        "OpenMP")
+
+
+def time_reference(step, n: int, warmup: int, max_steps: int, seconds: float):
+    """Warm-up steps, then timed steps until `max_steps` or `seconds`; (particle-steps/s,
+    steps, seconds)."""
+    for _ in range(max(1, warmup)):
+        step()
     steps, t0 = 0, time.perf_counter()
-    while True:
-        oracle.step(pos, vel, force, scene.params, ref_sort=True)
+    while steps < max_steps:
+        step()
         steps += 1
-        dt = time.perf_counter() - t0
-        if dt >= seconds or steps >= 50:
+        if time.perf_counter() - t0 >= seconds:
             break
-    return {"value": scene.n * steps / dt, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": f"{steps} full steps of the {scene.n}-particle scene ({dt:.1f} s)"}
+    dt = time.perf_counter() - t0
+    return n * steps / dt, steps, dt
+
+
+def cpu_baseline(seconds: float = 10.0):
+    """The reference's step on the host cores (reference_stepper) for about `seconds`."""
+    step, kind, threads, n, what = reference_stepper()
+    value, steps, dt = time_reference(step, n, 1, 50, seconds)
+    return {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"{steps} full steps of the {n}-particle scene on the reference's hash keys ({dt:.1f} s): "
+                      + what}
 
 
 def _time_steps(fn, steps: int, stream) -> float:
@@ -602,38 +671,31 @@ def profile_suite(stream) -> None:
 
 
 def run_reference(args, rank, world):
-    """--impl reference: the CPU port of the reference kernels (OpenMP over all host threads,
-    restated 4-bit reference sort) on the full 1M scene: `--warmup` untimed steps, then the
-    timed steps, at most 600 of them (about a minute) or as many as fit in 120 s."""
+    """--impl reference: the reference's own step on the host cores (reference_stepper; the
+    product library is not loaded) on the full 1M scene: `--warmup` untimed steps, then the
+    timed steps, at most `--steps` or as many as fit in 120 s. Beside it, the oracle port's
+    rate on a 20 s sample of the same scene."""
     if rank != 0:
         return 0
-    import oracle
-    from libcl_gb300.scenes import block_collapse_3d
-    sc = block_collapse_3d()
-    pos, vel, force = sc.pos.copy(), sc.vel.copy(), np.zeros_like(sc.pos)
-    for _ in range(max(1, args.warmup)):
-        oracle.step(pos, vel, force, sc.params, ref_sort=True)
-    steps, t0 = 0, time.perf_counter()
-    while steps < min(args.steps, 600):
-        oracle.step(pos, vel, force, sc.params, ref_sort=True)
-        steps += 1
-        if time.perf_counter() - t0 > 120.0:
-            break
-    dt = time.perf_counter() - t0
-    value = sc.n * steps / dt
-    cores = oracle.num_threads()
-    sample = f"{steps} full steps of the {sc.n}-particle scene after {max(1, args.warmup)} warm-up steps"
+    step, kind, threads, n, what = reference_stepper()
+    value, steps, dt = time_reference(step, n, args.warmup, args.steps, 120.0)
+    sample = f"{steps} full steps of the {n}-particle scene after {max(1, args.warmup)} warm-up steps: {what}"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded jittered lattice, block_collapse_3d seed 2)",
-        "config": {"workload": "3d_block_collapse_1M", "particles": sc.n, "lattice": [128, 64, 128],
-                   "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "config": workload_config(world),
+        "keys": "reference hash (262,144 buckets), 4-bit block radix sort",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
+    if kind == "reference":
+        pstep, _, pthreads, _, pwhat = reference_stepper(prefer_reference=False)
+        pvalue, psteps, pdt = time_reference(pstep, n, 1, 50, 20.0)
+        line["port"] = {"value": pvalue, "unit": UNIT, "cores": pthreads, "kind": "port",
+                        "sample": f"{psteps} full steps ({pdt:.1f} s): {pwhat}"}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -724,10 +786,10 @@ def main(argv=None) -> int:
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded jittered lattice, block_collapse_3d seed 2)",
-        "config": {"workload": "3d_block_collapse_1M", "particles": scene.n, "lattice": [128, 64, 128],
-                   "grid": [200, 100, 200], "h": 0.02, "dt": 5e-5, "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed steps (512 MiB write)", "graph": True,
-                   "keys": args.keys},
+        "config": workload_config(world),
+        "keys": ("linear grid 200x100x200, 3 x 8-bit one-sweep passes" if args.keys == "linear" else
+                 "reference hash (262,144 buckets), exact kernels"),
+        "graph": True,
         "gpu_launches": launches_per_step * args.steps,
         "step_ms_p50": statistics.median(step_ms),
     }
@@ -757,12 +819,18 @@ def main(argv=None) -> int:
         dom_bytes = STAGE_BYTES_PER_PARTICLE[dom] * scene.n
         ach = stage_gbs[dom]
         if args.keys == "linear":  # byte and flop counts of the linear-grid step's kernels
-            traffic = None
+            # DRAM bytes of one launch from the committed ncu capture named in the file (not
+            # measured in this run)
+            traffic, traffic_src = None, None
             tp = ROOT / "profiles" / "traffic.json"
             if tp.exists():
-                traffic = json.loads(tp.read_text()).get(dom)
+                rec = json.loads(tp.read_text()).get(dom)
+                if rec:
+                    traffic = rec["dram_bytes_per_launch"]
+                    traffic_src = f"ncu, {rec['profile']} (kernels of commit {rec['commit']})"
             result["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
                                   "frac": ach / peak, "peak_source": peak_kind, "traffic": traffic,
+                                  "traffic_source": traffic_src,
                                   "algorithmic_bytes_per_launch": dom_bytes, "avg_launch_ms": stage_ms[dom]}
             fl = neighbour_flops(fluid, scene.params)
             fp32_peak = sm_count(torch) * 128 * 2 * (result["clocks"].get("sm_mhz") or 2070.0) * 1e6 / 1e12
@@ -773,7 +841,7 @@ def main(argv=None) -> int:
                 fl[f"{stg}_achieved_tflops"] = tf
                 fl[f"{stg}_fp32_frac"] = tf / fp32_peak
             result["flops"] = fl
-        step_bytes = sum(STAGE_BYTES_PER_PARTICLE.values()) * scene.n + 8 * n_cells_occ
+        step_bytes = sum(STAGE_BYTES_PER_PARTICLE.values()) * scene.n + 8 * TABLE_CELLS + 8 * n_cells_occ
         result["stages"] = {"ms": stage_ms, "gbs": stage_gbs, "occupied_cells": n_cells_occ,
                             "step_algorithmic_bytes": step_bytes,
                             "step_hbm_frac": step_bytes / (t_ms / args.steps * 1e-3) / 1e9 / peak}
@@ -808,7 +876,7 @@ def main(argv=None) -> int:
                                 "bvh_1m_triangles": extra_bvh(stream),
                                 "bvh_lines_1m_segments": extra_bvh_lines(stream)}
         if world == 1 and not args.no_cpu_baseline:
-            result["cpu_baseline"] = cpu_baseline(scene, args.cpu_seconds)
+            result["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:

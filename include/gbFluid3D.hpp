@@ -158,7 +158,7 @@ class gbFluid3D {
     explicit gbFluid3D(gbContext& ctx)
         : mPosition(ctx, "bfPosition"), mVelocity(ctx, "bfVelocity"), mForce(ctx, "bfForce"),
           mSortedPosition(ctx, "bfSortedPosition"), mSortedVelocity(ctx, "bfSortedVelocity"),
-          mIndex(ctx, "bfIndex") {
+          mIndex(ctx, "bfIndex"), mParams(ctx, "bfParams") {
         gbStatus() = gbsph_fluid3d_create(&mH);
         rewrap();
     }
@@ -200,6 +200,16 @@ class gbFluid3D {
     gbBuffer& getSortedPositionBuffer() { return mSortedPosition; }
     gbBuffer& getSortedVelocityBuffer() { return mSortedVelocity; }
     gbBuffer& getIndexBuffer() { return mIndex; }
+    // getParamBuffer (libCL/phys/oclFluid3D.cpp:198-201): the device copy of getParameters()
+    // (one Params record; its first 13 fields are the kernels' System block), brought up to
+    // date by this call and by every compute() whose parameters changed.
+    gbBuffer& getParamBuffer() {
+        size_t count = 0;
+        void* p = mH ? gbsph_fluid3d_get_buffer(mH, GBSPH_BUF_PARAMS, &count) : nullptr;
+        mParams.wrap(p, count * sizeof(Params));
+        mParams.setOwner(this);
+        return mParams;
+    }
 
     Params& getParameters() { return *gbsph_fluid3d_get_params(mH); }
 
@@ -239,7 +249,7 @@ class gbFluid3D {
     }
 
     gbsph_fluid3d_t mH = nullptr;
-    gbBuffer mPosition, mVelocity, mForce, mSortedPosition, mSortedVelocity, mIndex;
+    gbBuffer mPosition, mVelocity, mForce, mSortedPosition, mSortedVelocity, mIndex, mParams;
     gbBuffer* mUser[3] = {nullptr, nullptr, nullptr};
     srtEvent* mHandler = nullptr;
     gbDevice* mDevice = nullptr;

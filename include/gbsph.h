@@ -54,11 +54,14 @@ GBSPH_API const char* gbsph_status_string(int status);
  *              1), so the next tile's decoupled look-back waits on a status word nobody
  *              writes;
  *   which = 1: a kernel that waits on a shared-memory mbarrier expecting bytes that no copy
- *              delivers.
+ *              delivers;
+ *   which = 2: the pass of which = 0 run inside the allocation-free sort's static array: it
+ *              returns without synchronising, and gbsph_radix_sort_noalloc_status reports
+ *              the timeout.
  * Each wait gives up after about one second, sets its device error bit and the kernel ends;
- * the call synchronises `stream` and returns GBSPH_ERR_DEVICE_TIMEOUT if that happened (and
- * the context stays usable), GBSPH_OK if the wait somehow completed, or an argument/CUDA
- * error. */
+ * for which = 0 and 1 the call synchronises `stream` and returns GBSPH_ERR_DEVICE_TIMEOUT if
+ * that happened (and the context stays usable), GBSPH_OK if the wait somehow completed, or
+ * an argument/CUDA error. */
 GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream);
 
 /* ABI version: major*10000 + minor*100 + patch. */
@@ -107,10 +110,18 @@ GBSPH_API const char* gbsph_radix_sort_last_error(gbsph_radix_sort_t h);
  * on cudaMalloc/cudaFree, plugins with a fixed memory footprint). Its scratch is a static
  * device array of about 5 MB that every GPU loading the library holds until exit.
  * Limits: at most 262,144 pairs (GBSPH_ERR_TOO_LARGE beyond); the first call on a device
- * looks up the array's address, so make it before any stream capture; all calls share the
- * array, so calls that overlap on the GPU race; device-side timeouts are not reported. */
+ * looks up the array's address, so make it before any stream capture, and do not reset the
+ * device (cudaDeviceReset) afterwards in the same process; all calls share the array, so
+ * calls that overlap on the GPU race. A device-side fault (a look-back wait that ran out)
+ * leaves the output undefined and is recorded in the array's error word until
+ * gbsph_radix_sort_noalloc_status reads it. */
 GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t n_keys,
                                        size_t n_values, int start_bit, int end_bit, void* stream);
+/* Status of the allocation-free sort (no counterpart in the reference): synchronises
+ * `stream`, then returns GBSPH_OK if no gbsph_radix_sort_noalloc call on the current device
+ * recorded a device-side fault since the last read, else that fault's status
+ * (GBSPH_ERR_DEVICE_TIMEOUT, GBSPH_ERR_STATE), and clears the record. Allocates nothing. */
+GBSPH_API int gbsph_radix_sort_noalloc_status(void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * 3D SPH fluid. Replaces `oclFluid3D` (libCL/phys/oclFluid3D.h:21-123,
@@ -164,7 +175,8 @@ enum {
     GBSPH_BUF_SORTED_POSITION = 3,
     GBSPH_BUF_SORTED_VELOCITY = 4,
     GBSPH_BUF_INDEX = 5,
-    GBSPH_BUF_CELL = 6
+    GBSPH_BUF_CELL = 6,
+    GBSPH_BUF_PARAMS = 7  /* one gbsph_fluid3d_params record on the device (getParamBuffer) */
 };
 
 /* Stages of one step, in the order `oclFluid3D::compute` enqueues them
@@ -219,7 +231,13 @@ GBSPH_API size_t gbsph_fluid3d_get_particle_count(gbsph_fluid3d_t h);
  * count >= N. Only POSITION, VELOCITY and FORCE are settable. */
 GBSPH_API int gbsph_fluid3d_set_buffer(gbsph_fluid3d_t h, int which, void* device_ptr,
                                        size_t count);
-/* get*Buffer -- libCL/phys/oclFluid3D.cpp:171-201. Returns the device pointer, or NULL. */
+/* get*Buffer -- libCL/phys/oclFluid3D.cpp:171-201. Returns the device pointer, or NULL.
+ * GBSPH_BUF_PARAMS is getParamBuffer (libCL/phys/oclFluid3D.cpp:198-201, a device buffer
+ * over the host Params, libCL/phys/oclFluid3D.cpp:58): one gbsph_fluid3d_params record
+ * (count = 1) whose first 13 fields are the reference's `System` block, so kernels written
+ * for it can bind it. The copy is brought up to date with the host struct by this call and,
+ * on the step's stream, by every compute() and stage() whose parameters changed; kernels an
+ * integrate hook enqueues see the parameters of the step that calls it. */
 GBSPH_API void* gbsph_fluid3d_get_buffer(gbsph_fluid3d_t h, int which, size_t* count);
 /* getParameters -- libCL/phys/oclFluid3D.cpp:204-207. Host-side struct, read at every
  * compute(); edit it in place. */

@@ -32,7 +32,7 @@ ERR_STATE = -10
 KEY_REFERENCE_HASH = 0
 KEY_LINEAR_GRID = 1
 
-BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY, BUF_INDEX, BUF_CELL = range(7)
+BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY, BUF_INDEX, BUF_CELL, BUF_PARAMS = range(8)
 (STAGE_HASH, STAGE_SORT, STAGE_REORDER, STAGE_BOUNDS, STAGE_DENSITY, STAGE_FORCES, STAGE_CLIP_BOX,
  STAGE_INTEGRATE_FORCE, STAGE_GRAVITY, STAGE_INTEGRATE_VELOCITY) = range(10)
 OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE = range(4)
@@ -86,6 +86,7 @@ SIGNATURES = {
     "gbsph_radix_sort_sync_status": (_I, [_P, _P]),
     "gbsph_radix_sort_last_error": (C.c_char_p, [_P]),
     "gbsph_radix_sort_noalloc": (_I, [_P, _P, _SZ, _SZ, _I, _I, _P]),
+    "gbsph_radix_sort_noalloc_status": (_I, [_P]),
     "gbsph_fluid3d_create": (_I, [C.POINTER(_P)]),
     "gbsph_fluid3d_destroy": (_I, [_P]),
     "gbsph_fluid3d_compile": (_I, [_P]),
@@ -344,6 +345,9 @@ class Fluid3D:
         if which in self._borrowed:
             return self._borrowed[which]
         n = count.value
+        if which == BUF_PARAMS:  # one gbsph_fluid3d_params record, as float32 words
+            words = C.sizeof(Fluid3DParams) // 4
+            return _device_view(p, words, torch.float32, (words,))
         is_f4 = which in (BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY)
         return _device_view(p, n * 4 if is_f4 else n, torch.float32 if is_f4 else torch.int32,
                             (n, 4) if is_f4 else (n,))
@@ -368,6 +372,12 @@ class Fluid3D:
 
     def getCellBuffer(self):
         return self.buffer(BUF_CELL)
+
+    def getParamBuffer(self):
+        """getParamBuffer (libCL/phys/oclFluid3D.cpp:198-201): a float32 view of the device copy
+        of getParameters() (first 13 words: the kernels' System block), brought up to date by
+        this call and by every compute() whose parameters changed."""
+        return self.buffer(BUF_PARAMS)
 
     def cell_bounds(self, n_cells: int, stream=None):
         import torch

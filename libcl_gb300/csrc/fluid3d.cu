@@ -96,12 +96,32 @@ struct gbsph_fluid3d_s {
     cudaEvent_t io_ev[3] = {};  // fork, velocity uploaded, force uploaded
     cudaGraphExec_t gexec_io = nullptr;
     std::vector<char> gkey_io;
+    // getParamBuffer: a device copy of `params`, refreshed on the stream before a step whenever
+    // the host struct differs from the copy last written (`dparams_shadow`)
+    gbsph_fluid3d_params* dparams = nullptr;
+    gbsph_fluid3d_params dparams_shadow{};
+    bool dparams_valid = false;
     std::string last_error;
 };
 
 namespace {
 
 using H = gbsph_fluid3d_s;
+
+__global__ void k_store_params(gbsph_fluid3d_params* __restrict__ out, gbsph_fluid3d_params p) {
+    if (threadIdx.x == 0) *out = p;
+}
+
+// Brings the device copy of the parameters up to date on `s` (no-op when unchanged). The
+// struct travels as a kernel argument, so later host edits cannot race with the write.
+int refresh_param_buffer(H* h, cudaStream_t s) {
+    if (h->dparams_valid && std::memcmp(&h->dparams_shadow, &h->params, sizeof(h->params)) == 0) return GBSPH_OK;
+    k_store_params<<<1, 32, 0, s>>>(h->dparams, h->params);
+    GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+    h->dparams_shadow = h->params;
+    h->dparams_valid = true;
+    return GBSPH_OK;
+}
 
 void default_params(gbsph_fluid3d_params* p) {
     // clInitFluid, libCL/phys/oclFluid3D.cl:130-148 (double literals evaluated in double)
@@ -633,6 +653,8 @@ GBSPH_API int gbsph_fluid3d_create(gbsph_fluid3d_t* out) {
     if (!rc && cudaMalloc(&h->err, 256) != cudaSuccess) rc = GBSPH_ERR_CUDA;
     if (!rc && cudaMemset(h->err, 0, 256) != cudaSuccess) rc = GBSPH_ERR_CUDA;
     if (!rc && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc && cudaMalloc(&h->dparams, sizeof(gbsph_fluid3d_params)) != cudaSuccess) rc = GBSPH_ERR_CUDA;
+    if (!rc && cudaMemset(h->dparams, 0, sizeof(gbsph_fluid3d_params)) != cudaSuccess) rc = GBSPH_ERR_CUDA;
     if (!rc) rc = alloc_particle_arrays(h, h->n);
     for (int w = 0; w < 3 && !rc; w++) rc = alloc_owned(h, w, h->n);
     if (rc) {
@@ -656,6 +678,7 @@ GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h) {
     if (h->xlist) cudaFree(h->xlist);
     if (h->table) cudaFree(h->table);
     if (h->err) cudaFree(h->err);
+    if (h->dparams) cudaFree(h->dparams);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     if (h->io_stream) cudaStreamDestroy(h->io_stream);
     for (auto e : h->io_ev)
@@ -671,6 +694,8 @@ GBSPH_API int gbsph_fluid3d_compile(gbsph_fluid3d_t h) {
     GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
     default_params(&h->params);
     RC(setup_kernels(h));
+    RC(refresh_param_buffer(h, nullptr));
+    GBSPH_CUDA_TRY(&h->last_error, cudaStreamSynchronize(nullptr));
     h->compiled = true;
     return GBSPH_OK;
 }
@@ -729,6 +754,14 @@ GBSPH_API void* gbsph_fluid3d_get_buffer(gbsph_fluid3d_t h, int which, size_t* c
         case GBSPH_BUF_SORTED_VELOCITY: p = h->svel; break;
         case GBSPH_BUF_INDEX: p = h->index; break;
         case GBSPH_BUF_CELL: p = h->keys_c; break;
+        case GBSPH_BUF_PARAMS:  // one record, brought up to date with the host struct first
+            if (cudaSetDevice(h->device) != cudaSuccess || refresh_param_buffer(h, nullptr) != GBSPH_OK ||
+                cudaStreamSynchronize(nullptr) != cudaSuccess) {
+                cudaGetLastError();
+                return nullptr;
+            }
+            if (count) *count = 1;
+            return h->dparams;
         default: return nullptr;
     }
     if (count) *count = h->n;
@@ -779,6 +812,7 @@ int compute_impl(H* h, cudaStream_t s, const HostIO* io, bool io_graph) {
     RC(validate_params(h));
     GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
     RC(ensure_tables(h));
+    RC(refresh_param_buffer(h, s));
     const KParams kp = make_kparams(h);
     const size_t bytes = (size_t)kp.n * 16;
     if (!h->opt_fused) {
@@ -877,6 +911,7 @@ GBSPH_API int gbsph_fluid3d_stage(gbsph_fluid3d_t h, int stage, void* stream) {
     RC(validate_params(h));
     GBSPH_CUDA_TRY(&h->last_error, cudaSetDevice(h->device));
     RC(ensure_tables(h));
+    RC(refresh_param_buffer(h, (cudaStream_t)stream));
     const KParams kp = make_kparams(h);
     cudaStream_t s = (cudaStream_t)stream;
     h->table_clean = false;

@@ -522,10 +522,13 @@ GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream) {
     return GBSPH_OK;
 }
 
+int selftest_noalloc_timeout(cudaStream_t s);  // below, beside the static scratch array
+
 GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream) {
-    if (which != 0 && which != 1) return GBSPH_ERR_ARGUMENT;
+    if (which < 0 || which > 2) return GBSPH_ERR_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
     if (which == 1) return selftest_mbarrier_timeout(s);
+    if (which == 2) return selftest_noalloc_timeout(s);
     // Two tiles of 2048 keys; the pass's tile counter starts at 1, so tile 0 never runs, the
     // CTA that draws tile 1 looks back at tile 0's unwritten status until its bound expires,
     // and the CTA that draws tile 2 finds no tile (a capacity error). The outputs stay inside
@@ -597,7 +600,9 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of g_noalloc_scratch on the current device, looked up once per device.
+// Device address of g_noalloc_scratch on the current device, looked up once per device (the
+// first call on a device does the lookup; a cudaDeviceReset later in the process would leave
+// the stored address stale, so the no-alloc entry points do not support one).
 cudaError_t noalloc_scratch(int device, void** out) {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[device]) {
@@ -610,7 +615,46 @@ cudaError_t noalloc_scratch(int device, void** out) {
     return cudaSuccess;
 }
 
+// The current device's scratch address (looked up on first use), or a status code.
+int noalloc_base(char** base) {
+    int device = 0;
+    GBSPH_CUDA_TRY(nullptr, cudaGetDevice(&device));
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES)
+        return fail(nullptr, GBSPH_ERR_ARGUMENT, "noalloc sort: device ordinal too large");
+    void* p = nullptr;
+    GBSPH_CUDA_TRY(nullptr, noalloc_scratch(device, &p));
+    *base = (char*)p;
+    return GBSPH_OK;
+}
+
 }  // namespace
+
+// gbsph_selftest_bounded_wait(2): selftest (0)'s timed-out pass run inside the static scratch
+// array (two 2048-key tiles whose keys, outputs, histogram and look-back words all lie in the
+// array), recording the timeout in the array's error word, where
+// gbsph_radix_sort_noalloc_status finds it. Asynchronous on `s`; allocates nothing.
+int selftest_noalloc_timeout(cudaStream_t s) {
+    char* b = nullptr;
+    int rc = noalloc_base(&b);
+    if (rc) return rc;
+    constexpr int ITEMS = 8;
+    const uint32_t n = 2 * SORT_THREADS * ITEMS, tiles = 2;
+    static_assert(2 * SORT_THREADS * 8 * 3 <= 4 * NOALLOC_MAX_KEYS, "selftest keys fit the array");
+    uint32_t* scratch = (uint32_t*)b;
+    uint32_t* keys = (uint32_t*)(b + NOALLOC_TMP_OFFSET);
+    uint32_t* kout = keys + n;
+    uint32_t* vout = kout + n;
+    uint32_t* err = (uint32_t*)(b + NOALLOC_ERR_OFFSET);
+    static const uint32_t one = 1;
+    SortGather g{};
+    GBSPH_CUDA_TRY(nullptr, cudaMemsetAsync(b, 0, SORT_HEADER_BYTES + (size_t)tiles * SORT_RADIX * 4, s));
+    GBSPH_CUDA_TRY(nullptr, cudaMemsetAsync(keys, 0, 3ull * n * 4, s));
+    GBSPH_CUDA_TRY(nullptr, cudaMemcpyAsync(scratch + 4096 / 4, &one, 4, cudaMemcpyHostToDevice, s));
+    k_onesweep<true, 0, ITEMS><<<tiles, SORT_THREADS, 0, s>>>(keys, nullptr, kout, vout, n, 0, 8, 0, tiles, scratch, err,
+                                                              g);
+    GBSPH_CUDA_TRY(nullptr, cudaGetLastError());
+    return GBSPH_OK;
+}
 
 extern "C" {
 
@@ -622,7 +666,9 @@ extern "C" {
 // * every call on a device shares the one scratch array and the call clears it with
 //   cudaMemsetAsync on `stream`; calls that overlap on the GPU (different streams without
 //   ordering between them) race on it and must not be issued;
-// * a device-side look-back timeout leaves the output undefined and is not reported here.
+// * a device-side fault of the sort (a look-back wait that ran out, a tile-capacity error)
+//   leaves the output undefined and sets a bit in the array's error word, which stays set
+//   across calls until gbsph_radix_sort_noalloc_status reads and clears it.
 GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t n_keys, size_t n_values,
                                        int start_bit, int end_bit, void* stream) {
     if (n_keys != n_values) return fail(nullptr, GBSPH_ERR_SIZE_MISMATCH, "noalloc sort: key and value counts differ");
@@ -634,19 +680,15 @@ GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t 
         return fail(nullptr, GBSPH_ERR_BIT_RANGE, "noalloc sort: bit range must be a multiple of 4 within [0, 32]");
     if (n_keys == 0 || start_bit == end_bit) return GBSPH_OK;
     if (!keys || !values) return fail(nullptr, GBSPH_ERR_ARGUMENT, "noalloc sort: null key or value pointer");
-    int device = 0;
-    GBSPH_CUDA_TRY(nullptr, cudaGetDevice(&device));
-    if (device < 0 || device >= NOALLOC_MAX_DEVICES) return fail(nullptr, GBSPH_ERR_ARGUMENT, "noalloc sort: device ordinal too large");
-    void* base = nullptr;
-    GBSPH_CUDA_TRY(nullptr, noalloc_scratch(device, &base));
-    char* b = (char*)base;
+    char* b = nullptr;
+    int rc = noalloc_base(&b);
+    if (rc) return rc;
     const uint32_t n = (uint32_t)n_keys;
     const int P = sort_passes(start_bit, end_bit);
     cudaStream_t s = (cudaStream_t)stream;
     uint32_t* err = (uint32_t*)(b + NOALLOC_ERR_OFFSET);
     uint32_t* tmp = (uint32_t*)(b + NOALLOC_TMP_OFFSET);
     GBSPH_CUDA_TRY(nullptr, onesweep_prepare(b, n, P, s));  // histogram, counters, look-back words
-    GBSPH_CUDA_TRY(nullptr, cudaMemsetAsync(err, 0, 4, s));
     GBSPH_CUDA_TRY(nullptr, onesweep_histogram(keys, n, start_bit, end_bit, b, s));
     OnesweepArgs a;
     a.keys_in = keys;
@@ -672,6 +714,26 @@ GBSPH_API int gbsph_radix_sort_noalloc(uint32_t* keys, uint32_t* values, size_t 
         GBSPH_CUDA_TRY(nullptr, onesweep_passes(a, s));
     }
     return GBSPH_OK;
+}
+
+// Synchronises `stream`, then reads the static array's error word: GBSPH_OK when no no-alloc
+// sort on this device has recorded a device-side fault since the last read, else the fault's
+// status (GBSPH_ERR_DEVICE_TIMEOUT for a look-back wait that ran out, GBSPH_ERR_STATE for a
+// tile-capacity error), after which the word is cleared. Allocates nothing; like the sort, the
+// first call on a device looks up the array's address.
+GBSPH_API int gbsph_radix_sort_noalloc_status(void* stream) {
+    char* b = nullptr;
+    int rc = noalloc_base(&b);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t* err = (uint32_t*)(b + NOALLOC_ERR_OFFSET);
+    GBSPH_CUDA_TRY(nullptr, cudaStreamSynchronize(s));
+    uint32_t bits = 0;
+    GBSPH_CUDA_TRY(nullptr, cudaMemcpy(&bits, err, 4, cudaMemcpyDeviceToHost));
+    if (!bits) return GBSPH_OK;
+    GBSPH_CUDA_TRY(nullptr, cudaMemsetAsync(err, 0, 4, s));
+    GBSPH_CUDA_TRY(nullptr, cudaStreamSynchronize(s));
+    return fail(nullptr, dev_err_to_status(bits), "noalloc sort: device error word 0x" + std::to_string(bits));
 }
 
 }  // extern "C"

@@ -41,6 +41,7 @@ def lib() -> C.CDLL:
             "orc_stable_sort": (C.c_int, [P, P, U, C.c_int, C.c_int]),
             "orc_find_bounds": (C.c_int, [P, U, P, P, U]),
             "orc_init_fluid_params": (None, [P]),
+            "orc_kernel_constants": (None, [C.c_float, C.c_float, P]),
             "orc_hash": (None, [P, U, P, P, P]),
             "orc_reorder": (None, [P, P, P, P, P, U]),
             "orc_density": (None, [P, P, P, P, U, P]),
@@ -100,6 +101,13 @@ def find_bounds(sorted_keys: np.ndarray, n_cells: int):
 
 def init_fluid_params(params) -> None:
     lib().orc_init_fluid_params(_pp(params))
+
+
+def kernel_constants(cell_size: float, viscosity: float) -> np.ndarray:
+    """(kernelConstant, viscosityConstant, pressureConstant) by clInitFluid's formulas."""
+    out = np.zeros(3, np.float32)
+    lib().orc_kernel_constants(cell_size, viscosity, _p(out))
+    return out
 
 
 def table_cells(params) -> int:

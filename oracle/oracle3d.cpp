@@ -267,6 +267,18 @@ int orc_find_bounds(const uint32_t* cell, uint32_t n, uint32_t* cellStart, uint3
     return skipped;
 }
 
+// The kernel constants clInitFluid forms (libCL/phys/oclFluid3D.cl:145-147 with the macros
+// DensityConstant, ViscosityConstant, PressureConstant of :123-128) for a cell size h and a
+// viscosity mu: out = (kernelConstant, viscosityConstant, pressureConstant). M_PI_F is a
+// float: 64.0*M_PI_F is a double product, but M_PI_F * pow(h, 6.0f) is a float product,
+// divided into -45.0 in double.
+void orc_kernel_constants(float h, float mu, float* out) {
+    const float pi_f = 3.14159274101257f;  // M_PI_F
+    out[0] = (float)(315.0 / (64.0 * (double)pi_f * (double)std::pow(h, 9.0f)));
+    out[1] = (float)(-(double)mu * (-45.0 / (double)(pi_f * std::pow(h, 6.0f))));
+    out[2] = (float)(-(-45.0 / (double)(pi_f * std::pow(h, 6.0f))));
+}
+
 // clInitFluid, libCL/phys/oclFluid3D.cl:130-148 (double literals evaluated in double,
 // pow() of float arguments in float), plus the hard-coded kernel arguments of
 // libCL/phys/oclFluid3D.cpp:256-268.
@@ -282,12 +294,11 @@ void orc_init_fluid_params(gbsph_fluid3d_params* p) {
     p->spacing = (float)(0.87 * (double)std::pow(p->mass / p->density, 1 / 3.0f));
     p->particleRadius = (float)(0.5 * (double)p->spacing);
     p->cellSize = (float)(2.0 * (double)p->spacing);
-    // M_PI_F is a float: 64.0*M_PI_F is a double product, but M_PI_F * pow(h, 6.0f) (the
-    // pressure and viscosity constants) is a float product, divided into -45.0 in double.
-    const float pi_f = 3.14159274101257f;  // M_PI_F
-    p->kernelConstant = (float)(315.0 / (64.0 * (double)pi_f * (double)std::pow(p->cellSize, 9.0f)));
-    p->viscosityConstant = (float)(-(double)p->viscosity * (-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
-    p->pressureConstant = (float)(-(-45.0 / (double)(pi_f * std::pow(p->cellSize, 6.0f))));
+    float k[3];
+    orc_kernel_constants(p->cellSize, p->viscosity, k);
+    p->kernelConstant = k[0];
+    p->viscosityConstant = k[1];
+    p->pressureConstant = k[2];
     p->gravity[0] = -9.8f * 0.0f;
     p->gravity[1] = -9.8f * 0.0f;
     p->gravity[2] = -9.8f * 1.0f;

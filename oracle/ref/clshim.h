@@ -38,8 +38,8 @@
 //     turns barrier(...) into `co_await clc::barrier_point{}` and `return;` into
 //     `co_return;`); run_groups_coro() runs a work-group's work-items in local-id order up
 //     to each barrier in turn, which is what the barrier requires of a work-group. __local
-//     variables declared in a kernel body become `static thread_local` (one copy per
-//     executing host thread, shared by the work-group it is running).
+//     arrays declared in a kernel body live in per-host-thread storage (local_array), shared
+//     by the work-group the thread is running.
 // Work-groups of one launch run on OpenMP threads; the reference's kernels write disjoint
 // locations per work-item, so the results do not depend on the schedule.
 #pragma once
@@ -311,14 +311,22 @@ inline size_t get_local_size(uint d) { return d < wi.dims ? wi.lsize[d] : 1; }
 inline size_t get_num_groups(uint d) { return d < wi.dims ? wi.ngroups[d] : 1; }
 inline uint get_work_dim() { return wi.dims; }
 
-inline void set_item_1d(size_t global, size_t local, size_t group, size_t l) {
-    wi.dims = 1;
-    wi.gsize[0] = global;
-    wi.lsize[0] = local;
-    wi.ngroups[0] = global / local;
-    wi.grp[0] = group;
-    wi.lid[0] = l;
-    wi.gid[0] = group * local + l;
+// The calling thread's work-item record set to the first item of 1D work-group `group`
+// (one thread-local lookup; the caller then steps lid/gid through the group).
+inline work_item& enter_group_1d(size_t global, size_t local, size_t group) {
+    work_item& w = wi;
+    w.dims = 1;
+    w.gsize[0] = global;
+    w.lsize[0] = local;
+    w.ngroups[0] = global / local;
+    w.grp[0] = group;
+    w.lid[0] = 0;
+    w.gid[0] = group * local;
+    return w;
+}
+inline void set_local_id(work_item& w, size_t l) {
+    w.lid[0] = l;
+    w.gid[0] = w.grp[0] * w.lsize[0] + l;
 }
 
 // A kernel without barriers: every work-item of a 1D range, groups on OpenMP threads.
@@ -326,18 +334,20 @@ inline void set_item_1d(size_t global, size_t local, size_t group, size_t l) {
 template <class F>
 inline void run_groups(size_t global, size_t local, F&& f) {
     const long long groups = (long long)(global / local);
-#pragma omp parallel for schedule(static)
-    for (long long g = 0; g < groups; g++)
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long g = 0; g < groups; g++) {
+        work_item& w = enter_group_1d(global, local, (size_t)g);
         for (size_t l = 0; l < local; l++) {
-            set_item_1d(global, local, (size_t)g, l);
+            set_local_id(w, l);
             f();
         }
+    }
 }
 
 // A kernel without barriers over a 2D range (each work-item its own group).
 template <class F>
 inline void run_items_2d(size_t gx, size_t gy, F&& f) {
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(dynamic, 4)
     for (long long y = 0; y < (long long)gy; y++)
         for (size_t x = 0; x < gx; x++) {
             wi.dims = 2;
@@ -353,9 +363,46 @@ inline void run_items_2d(size_t gx, size_t gy, F&& f) {
         }
 }
 
-// Coroutine work-items for kernels with barriers.
+// Storage of one `__local T name[N]` declaration site for the work-group the calling host
+// thread is running (the source rewrite binds a reference to it once per work-item).
+template <class T, size_t N, int SITE>
+inline T (&local_array())[N] {
+    static thread_local T storage[N];
+    return storage;
+}
+
+// Coroutine work-items for kernels with barriers. Their frames come from a per-thread pool
+// (a work-group's items are created and destroyed together, thousands of times per launch).
+struct frame_pool {
+    std::vector<void*> free_blocks;
+    size_t block = 0;
+    ~frame_pool() {
+        for (void* p : free_blocks) ::operator delete(p);
+    }
+};
+inline thread_local frame_pool g_frames;
+
 struct wi_task {
     struct promise_type {
+        static void* operator new(size_t sz) {
+            frame_pool& fp = g_frames;
+            if (sz != fp.block) {  // a kernel with another frame size: start a new pool
+                for (void* p : fp.free_blocks) ::operator delete(p);
+                fp.free_blocks.clear();
+                fp.block = sz;
+            }
+            if (fp.free_blocks.empty()) return ::operator new(sz);
+            void* p = fp.free_blocks.back();
+            fp.free_blocks.pop_back();
+            return p;
+        }
+        static void operator delete(void* p, size_t sz) {
+            frame_pool& fp = g_frames;
+            if (sz == fp.block)
+                fp.free_blocks.push_back(p);
+            else
+                ::operator delete(p);
+        }
         wi_task get_return_object() { return wi_task{std::coroutine_handle<promise_type>::from_promise(*this)}; }
         std::suspend_never initial_suspend() noexcept { return {}; }
         std::suspend_always final_suspend() noexcept { return {}; }
@@ -377,18 +424,19 @@ struct barrier_point {
 template <class F>
 inline void run_groups_coro(size_t global, size_t local, F&& f) {
     const long long groups = (long long)(global / local);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(dynamic, 4)
     for (long long g = 0; g < groups; g++) {
         std::vector<wi_task> items(local);
+        work_item& w = enter_group_1d(global, local, (size_t)g);
         for (size_t l = 0; l < local; l++) {
-            set_item_1d(global, local, (size_t)g, l);
+            set_local_id(w, l);
             items[l] = f();
         }
         for (bool live = true; live;) {
             live = false;
             for (size_t l = 0; l < local; l++) {
                 if (items[l].h.done()) continue;
-                set_item_1d(global, local, (size_t)g, l);
+                set_local_id(w, l);
                 items[l].h.resume();
                 live = true;
             }

@@ -10,8 +10,11 @@ own lines through a #line directive):
    `clc::make<clc::float4>(a, b, c, d)`: in C++ the original parses as a cast of a comma
    expression and silently keeps only the last operand;
 3. `__local` in a parameter list is dropped (the runner passes one buffer per work-group);
-   `__local` inside a kernel body becomes `static thread_local` (shared by the work-group
-   that the host thread is running, as OpenCL's local memory is);
+   an array `__local T name[N];` inside a kernel body becomes a reference bound once per
+   work-item, `T (&name)[N] = clc::local_array<T, N, SITE>();`, to storage that the host
+   thread running the work-group owns (so it is shared by the work-group, as OpenCL's local
+   memory is, and later accesses need no thread-local lookup); any other `__local` inside a
+   body becomes `static thread_local`;
 4. a kernel whose body calls barrier() becomes a coroutine: its return type `void` becomes
    `clc::wi_task`, `barrier(...);` becomes `co_await clc::barrier_point{};` and `return;`
    becomes `co_return;`.
@@ -66,22 +69,37 @@ def _match(src: str, i: int, open_c: str, close_c: str) -> int:
     raise ValueError(f"unbalanced {open_c}{close_c} from offset {i}")
 
 
+_LOCAL_ARRAY = re.compile(r"__local\s+(\w+)\s+(\w+)\s*\[([^\]]+)\]\s*;")
+
+
 def _locals(src: str) -> str:
     out = []
     depth = 0
+    site = 0
     i = 0
     for m in re.finditer(r"[{}]|\b__local\b", src):
+        if m.start() < i:
+            continue
         out.append(src[i:m.start()])
         tok = m.group(0)
+        i = m.end()
         if tok == "{":
             depth += 1
             out.append(tok)
         elif tok == "}":
             depth -= 1
             out.append(tok)
+        elif depth == 0:
+            out.append("")
         else:
-            out.append("static thread_local" if depth > 0 else "")
-        i = m.end()
+            arr = _LOCAL_ARRAY.match(src, m.start())
+            if arr:
+                t, name, n = arr.groups()
+                site += 1
+                out.append(f"{t} (&{name})[{n}] = clc::local_array<{t}, ({n}), {site}>();")
+                i = arr.end()
+            else:
+                out.append("static thread_local")
     out.append(src[i:])
     return "".join(out)
 

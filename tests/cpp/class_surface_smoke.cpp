@@ -151,6 +151,32 @@ static int testFluid3D1(gbContext& ctx) {
     return 0;
 }
 
+// getParamBuffer (libCL/phys/oclFluid3D.cpp:198-201): the device copy of the parameters,
+// read through the buffer's map() as a caller that binds it to its own kernels sees it; a
+// host edit reaches it with the next compute().
+static int testParamBuffer(gbContext& ctx) {
+    typedef gbFluid3D::Params Params;
+    gbDevice& dev = ctx.getDevice(0);
+    gbFluid3D fluid(ctx);
+    CHECK(fluid.compile());
+    fluid.setParticleCount(1024);
+    CHECK(initParticles(fluid) == 0);
+    gbBuffer& pb = fluid.getParamBuffer();
+    CHECK(pb.devicePtr() != nullptr && pb.bytes() == sizeof(Params));
+    CHECK(pb.map(gbBuffer::MAP_READ));
+    CHECK(std::memcmp(pb.ptr<Params>(), &fluid.getParameters(), sizeof(Params)) == 0);
+    pb.unmap();
+    fluid.getParameters().viscosity = 2.5f;
+    CHECK(fluid.compute(dev));
+    cudaDeviceSynchronize();
+    CHECK(pb.map(gbBuffer::MAP_READ));  // the same device memory, not looked up again
+    CHECK(pb.ptr<Params>()->viscosity == 2.5f);
+    CHECK(std::memcmp(pb.ptr<Params>(), &fluid.getParameters(), sizeof(Params)) == 0);
+    pb.unmap();
+    std::printf("testParamBuffer completed\n");
+    return 0;
+}
+
 // oclFluid2D: compile, a dam-break block of particles in the default container, a border
 // image with a wall column, 20 steps; positions stay finite and inside the container.
 static int testFluid2D(gbContext& ctx) {
@@ -260,7 +286,7 @@ static int testBvh(gbContext& ctx) {
 
 int main() {
     gbContext ctx(0);
-    if (testRadixSort(ctx) || testFluid3D0(ctx) || testFluid3D1(ctx) || testFluid2D(ctx) || testBvh(ctx)) return 1;
+    if (testRadixSort(ctx) || testFluid3D0(ctx) || testFluid3D1(ctx) || testParamBuffer(ctx) || testFluid2D(ctx) || testBvh(ctx)) return 1;
     std::printf("OK\n");
     return 0;
 }

@@ -461,6 +461,35 @@ def test_disordered_2d_block_within_tolerance_and_brick_width_free(cuda):
             assert_bit_exact(gs[k], sb[k], f"{k} (brick width {bw})")
 
 
+def test_param_buffer_follows_the_host_parameters(cuda):
+    """getParamBuffer (libCL/phys/oclFluid3D.cpp:198-201): a device record equal to
+    getParameters(); a host edit reaches it with the next compute(), also when the step is a
+    replayed graph, and through a stage() call."""
+    import torch
+    from libcl_gb300 import STAGE_GRAVITY
+    sc = block_collapse_3d(16, 8, 16)
+    f = make_fluid(sc)
+    pb = f.getParamBuffer()
+    torch.cuda.synchronize()
+
+    def host_words():
+        return np.frombuffer(bytes(f.getParameters()), np.float32)
+
+    assert np.array_equal(pb.cpu().numpy().view(np.uint32), host_words().view(np.uint32))
+    for _ in range(3):  # the third step replays the captured graph
+        f.compute()
+    f.getParameters().viscosity = 0.07
+    f.compute()
+    torch.cuda.synchronize()
+    assert pb.cpu().numpy()[4] == np.float32(0.07)
+    assert np.array_equal(pb.cpu().numpy().view(np.uint32), host_words().view(np.uint32))
+    f.getParameters().stiffness = 2.5
+    f.stage(STAGE_GRAVITY)
+    torch.cuda.synchronize()
+    assert pb.cpu().numpy()[8] == np.float32(2.5)
+    assert f.sync_status() == OK
+
+
 def test_emitter(cuda):
     """clEmitter (libCL/phys/oclFluid3D.cl:273-282): particles emit+1 .. emit+99 move to the
     sheet, the rest keep their state (expected values: fluid_helpers.emitter_expected, which

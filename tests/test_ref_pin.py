@@ -13,8 +13,6 @@ The shim fixes what OpenCL leaves to the implementation as the oracle does (fast
 length as sqrtf of the left-to-right sum of squares, IEEE division, pow(x, 3.0f) as x*x*x);
 test_pow_convention_moves_density_by_ulps measures what the pow choice changes.
 """
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -90,13 +88,16 @@ def test_init_fluid_defaults_match_the_reference():
 
 @pytest.mark.parametrize("h,mu", [(0.02, 0.05), (0.0316179, 6.0), (0.01, 0.1), (0.05, 0.2), (0.0173, 0.01)])
 def test_kernel_constants_match_the_reference_macros(h, mu):
-    """gbsph_fluid3d_params_derive against DensityConstant / PressureConstant /
-    ViscosityConstant as clInitFluid applies them (libCL/phys/oclFluid3D.cl:123-147)."""
+    """gbsph_fluid3d_params_derive and the oracle's restatement against DensityConstant /
+    PressureConstant / ViscosityConstant as clInitFluid applies them
+    (libCL/phys/oclFluid3D.cl:123-147)."""
     p = gb.Fluid3DParams()
     p.cellSize, p.viscosity, p.dims = h, mu, 3
     gb.params_derive(p)
     got = np.array([p.kernelConstant, p.viscosityConstant, p.pressureConstant], np.float32)
-    assert_same_bits(got, ref.kernel_constants(np.float32(h), np.float32(mu)), "kernel constants")
+    want = ref.kernel_constants(np.float32(h), np.float32(mu))
+    assert_same_bits(got, want, "library kernel constants")
+    assert_same_bits(oracle.kernel_constants(np.float32(h), np.float32(mu)), want, "oracle kernel constants")
 
 
 def _hash_mode(params, gravity_arg):
