@@ -87,3 +87,50 @@ def test_autotune_restores_state(cuda):
     bt.compute()
     torch.cuda.synchronize()
     assert bt.sync_status() == 0
+
+
+def test_full_ensemble_against_oracle_and_scenes_run_alone(cuda):
+    """The batched configuration at full size: 256 scenes of 4,096-262,144 particles
+    (log-uniform, seed 5), one batched step from a perturbed state. Eight scenes across the
+    size range are compared with the oracle's step (oracle.step on the scene alone) within
+    RTOL: density, velocity and position; every one of the 256 scenes is bitwise equal to the
+    same scene run alone through Fluid3D."""
+    import torch
+    import oracle
+    from fluid_helpers import RTOL, pos_err, rel_err
+    from libcl_gb300 import BUF_SORTED_POSITION
+    b = batched_ensemble()
+    assert len(b.descs) == 256 and b.n > 15_000_000
+    rng = np.random.default_rng(6)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    bt = load_batch(b, bw=16)
+    bt.compute()
+    torch.cuda.synchronize()
+    assert bt.sync_status() == 0
+    got = {k: bt.buffer(w).cpu().numpy() for k, w in (("pos", BUF_POSITION), ("vel", BUF_VELOCITY), ("force", BUF_FORCE))}
+    idx = bt.buffer(BUF_INDEX).cpu().numpy().view(np.uint32)
+    rho = np.empty(b.n, np.float32)
+    rho[idx] = bt.buffer(BUF_SORTED_POSITION)[:, 3].cpu().numpy()
+    del bt
+    torch.cuda.empty_cache()
+    sizes = np.array([d.n_particles for d in b.descs])
+    picked = [int(np.argsort(sizes)[k]) for k in np.linspace(0, len(sizes) - 1, 8).astype(int)]
+    for s in range(len(b.descs)):
+        sc = b.scene(s)
+        a, n = b.firsts[s], sc.n
+        f = make_fluid(sc, vel=sc.vel)
+        f.set_option(OPT_BRICK_WIDTH, 16)
+        f.compute()
+        ref = state(f)
+        for k in ("pos", "vel", "force"):
+            assert np.array_equal(got[k][a:a + n].view(np.uint32), ref[k].view(np.uint32)), (s, k)
+        del f
+        if s in picked:
+            pos, vel, force = sc.pos.copy(), sc.vel.copy(), np.zeros_like(sc.pos)
+            r = oracle.step(pos, vel, force, sc.params)
+            rho_o = np.empty(n, np.float32)
+            rho_o[r.index] = r.spos[:, 3]
+            assert rel_err(rho[a:a + n], rho_o) <= RTOL, (s, "density")
+            assert rel_err(got["vel"][a:a + n], vel) <= RTOL, (s, "velocity")
+            assert pos_err(got["pos"][a:a + n], pos, sc.pos) <= 1.0, (s, "position")
+            assert np.array_equal(got["force"][a:a + n], force), (s, "force (gravity seed)")
