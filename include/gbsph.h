@@ -200,9 +200,6 @@ enum {
     GBSPH_OPT_FUSED = 0,      /* 1 (default): fused kernels; 0: one kernel per reference stage */
     GBSPH_OPT_CUDA_GRAPH = 1, /* 1 (default): replay the step as a captured CUDA graph */
     GBSPH_OPT_BRICK_WIDTH = 2, /* LINEAR_GRID neighbour bricks: cells per brick along x (1..16) */
-    GBSPH_OPT_NEIGHBOUR_LISTS = 4, /* LINEAR_GRID neighbour passes: 0 (default) in-range bitmasks
-                                      between the cell kernels, 1 16-bit staged-index lists
-                                      between the brick kernels */
     GBSPH_OPT_PROFILE = 3      /* 1: compute() runs eagerly and records a CUDA event pair per
                                   stage (the reference's CL_QUEUE_PROFILING_ENABLE events,
                                   libCL/oclDevice.cpp:31, libCL/oclKernel.cpp:162-202) */

@@ -35,7 +35,7 @@ KEY_LINEAR_GRID = 1
 BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY, BUF_INDEX, BUF_CELL, BUF_PARAMS = range(8)
 (STAGE_HASH, STAGE_SORT, STAGE_REORDER, STAGE_BOUNDS, STAGE_DENSITY, STAGE_FORCES, STAGE_CLIP_BOX,
  STAGE_INTEGRATE_FORCE, STAGE_GRAVITY, STAGE_INTEGRATE_VELOCITY) = range(10)
-OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE, OPT_NEIGHBOUR_LISTS = range(5)
+OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE = range(4)
 STAGE_TIME_NAMES = ("front_end", "sort", "bounds", "density", "forces")
 
 REF_BUCKETS = 262144  # cBucketCount, libCL/phys/oclFluid3D.cpp:17

@@ -13,7 +13,7 @@
 #include <string>
 #include <vector>
 
-#include "cell_kernels.cuh"
+#include "fluid3d_kernels.cuh"
 
 using namespace gbsph;
 
@@ -30,13 +30,12 @@ struct gbsph_batch3d_s {
     uint32_t *index = nullptr, *bricks = nullptr;
     uint16_t* nbr = nullptr;
     uint64_t* nbr_meta = nullptr;
-    uint32_t* masks = nullptr;
     uint2* table = nullptr;
     bool table_clean = false;
     void* scratch = nullptr;
     uint32_t* err = nullptr;
-    int bw = 8, use_graph = 1, sdev_bw = -1, lists = 0;
-    int dens_blocks = 0, force_blocks = 0, dens_cells_blocks = 0, force_cells_blocks = 0;
+    int bw = 8, use_graph = 1, sdev_bw = -1;
+    int dens_blocks = 0, force_blocks = 0;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
     std::vector<char> gkey;
@@ -162,18 +161,11 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     k_bounds_batch<<<(kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, bcounters(h), h->err);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     h->table_clean = true;
-    if (!h->lists) {
-        k_density_cells<3, true><<<h->dens_cells_blocks, BRICK_THREADS, DENSITY_CELLS_SMEM, s>>>(
-            h->spos, h->svel, h->table, h->bricks, bcounters(h), kp, h->masks, h->err);
-        k_force_cells<3, true, true><<<h->force_cells_blocks, BRICK_THREADS, FORCE_CELLS_SMEM, s>>>(
-            h->spos, h->svel, h->index, h->pos, h->vel, h->force, h->table, h->bricks, bcounters(h), kp, h->masks, h->err);
-    } else {
-        k_density_brick<3, true><<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(
-            h->spos, h->svel, h->table, h->bricks, bcounters(h), kp, h->nbr, h->nbr_meta, h->err);
-        k_force_brick<3, true, true><<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(
-            h->spos, h->svel, h->index, h->pos, h->vel, h->force, h->table, h->bricks, bcounters(h), kp, h->nbr,
-            h->nbr_meta, h->err);
-    }
+    k_density_brick<3, true><<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks,
+                                                                                bcounters(h), kp, h->nbr, h->nbr_meta, h->err);
+    k_force_brick<3, true, true><<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(
+        h->spos, h->svel, h->index, h->pos, h->vel, h->force, h->table, h->bricks, bcounters(h), kp, h->nbr, h->nbr_meta,
+        h->err);
     GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
     return GBSPH_OK;
 }
@@ -241,18 +233,6 @@ GBSPH_API int gbsph_batch3d_create(gbsph_batch3d_t* out) {
         if (!rc && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true, true>, BRICK_THREADS, FORCE_SMEM))
             rc = GBSPH_ERR_CUDA;
         h->force_blocks = std::max(1, nb) * sms;
-        if (!rc && (cudaFuncSetAttribute(k_density_cells<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)DENSITY_CELLS_SMEM) ||
-                    cudaFuncSetAttribute(k_force_cells<3, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)FORCE_CELLS_SMEM) ||
-                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_cells<3, true>, BRICK_THREADS,
-                                                                  DENSITY_CELLS_SMEM)))
-            rc = GBSPH_ERR_CUDA;
-        h->dens_cells_blocks = std::max(1, nb) * sms;
-        if (!rc && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_cells<3, true, true>, BRICK_THREADS,
-                                                                 FORCE_CELLS_SMEM))
-            rc = GBSPH_ERR_CUDA;
-        h->force_cells_blocks = std::max(1, nb) * sms;
     }
     if (rc) {
         cudaGetLastError();
@@ -323,7 +303,7 @@ GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_pa
     h->n = n;
     h->cells = cells;
     const size_t n4 = (n + 63) & ~size_t(63);
-    const size_t bytes = n4 * (5 * 16 + 7 * 4 + NBR_CAP * 2 + 8 + MASK_WORDS * 4) + 64;
+    const size_t bytes = n4 * (5 * 16 + 7 * 4 + NBR_CAP * 2 + 8);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->block, bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->block, 0, bytes));
     char* p = (char*)h->block;
@@ -340,8 +320,6 @@ GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_pa
     h->nbr = (uint16_t*)p;
     p += n4 * NBR_CAP * 2;
     h->nbr_meta = (uint64_t*)p;
-    p += n4 * 8;
-    h->masks = (uint32_t*)p;  // + 64 bytes of slack: the force pass copies whole 16-byte chunks
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->table, cells * sizeof(uint2)));
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES)));
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->sdev, n_scenes * sizeof(SceneDev)));
@@ -379,8 +357,6 @@ GBSPH_API int gbsph_batch3d_set_option(gbsph_batch3d_t h, int option, int value)
     } else if (option == GBSPH_OPT_BRICK_WIDTH) {
         if (value < 1 || value > BRICK_W_MAX) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "brick width must be in [1, 16]");
         h->bw = value;
-    } else if (option == GBSPH_OPT_NEIGHBOUR_LISTS) {
-        h->lists = value ? 1 : 0;
     } else {
         return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown option");
     }

@@ -68,7 +68,6 @@ struct gbsph_fluid3d_s {
     uint32_t *vals_a = nullptr, *vals_b = nullptr, *index = nullptr, *bricks = nullptr;
     uint16_t* nbr = nullptr;      // per particle NBR_CAP neighbour slots (density -> forces)
     uint64_t* nbr_meta = nullptr;  // per particle: sub-list lengths, scan flag (bit 63)
-    uint32_t* masks = nullptr;     // per particle MASK_WORDS in-range masks (cell kernels)
     uint32_t* hash_tables = nullptr;  // cell start / end, REF_BUCKETS each
     uint32_t* xlist = nullptr;        // REFERENCE_HASH fused step: XL_CAP neighbours + count per particle
     size_t xlist_n = 0;
@@ -85,10 +84,10 @@ struct gbsph_fluid3d_s {
     uint32_t rec_n4 = 0;
     gbsph_fluid3d_hook_fn hook = nullptr;
     void* hook_user = nullptr;
-    int opt_fused = 1, opt_graph = 1, opt_bw = 16, opt_profile = 0, opt_lists = 0;
+    int opt_fused = 1, opt_graph = 1, opt_bw = 16, opt_profile = 0;
     cudaEvent_t ev[6] = {};
     bool ev_valid = false;
-    int dens_blocks = 0, force_blocks = 0, dens_cells_blocks = 0, force_cells_blocks = 0;
+    int dens_blocks = 0, force_blocks = 0;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
     std::vector<char> gkey;
@@ -248,7 +247,7 @@ void free_particle_arrays(H* h) {
 int alloc_particle_arrays(H* h, size_t n) {
     free_particle_arrays(h);
     const size_t n4 = (n + 63) & ~size_t(63);
-    const size_t bytes = n4 * (2 * 16 + 7 * 4 + NBR_CAP * 2 + 8 + MASK_WORDS * 4) + 64;
+    const size_t bytes = n4 * (2 * 16 + 7 * 4 + NBR_CAP * 2 + 8);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->pblock, bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->pblock, 0, bytes));
     char* p = (char*)h->pblock;
@@ -264,8 +263,6 @@ int alloc_particle_arrays(H* h, size_t n) {
     h->nbr = (uint16_t*)p;
     p += n4 * NBR_CAP * 2;
     h->nbr_meta = (uint64_t*)p;
-    p += n4 * 8;
-    h->masks = (uint32_t*)p;  // + 64 bytes of slack: the force pass copies whole 16-byte chunks
     h->scratch_bytes = onesweep_scratch_bytes((uint32_t)n, SORT_MAX_PASSES);
     GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->scratch, h->scratch_bytes));
     GBSPH_CUDA_TRY(&h->last_error, cudaMemset(h->scratch, 0, h->scratch_bytes));
@@ -417,16 +414,6 @@ int st_forces_exact(H* h, const KParams& kp, cudaStream_t s, bool lists = false)
 }
 
 int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
-    if (!h->opt_lists) {
-        auto launch = [&](auto kern) {
-            kern<<<h->dens_cells_blocks, BRICK_THREADS, DENSITY_CELLS_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks,
-                                                                             counters(h), kp, h->masks, h->err);
-        };
-        if (kp.dims == 2) launch(k_density_cells<2, false>);
-        else launch(k_density_cells<3, false>);
-        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
-        return GBSPH_OK;
-    }
     auto launch = [&](auto kern) {
         kern<<<h->dens_blocks, BRICK_THREADS, DENSITY_SMEM, s>>>(h->spos, h->svel, h->table, h->bricks, counters(h), kp,
                                                                  h->nbr, h->nbr_meta, h->err);
@@ -438,22 +425,6 @@ int st_density_brick(H* h, const KParams& kp, cudaStream_t s) {
 }
 
 int st_force_brick(H* h, const KParams& kp, cudaStream_t s, bool fused) {
-    if (!h->opt_lists) {
-        auto launch = [&](auto kern) {
-            kern<<<h->force_cells_blocks, BRICK_THREADS, FORCE_CELLS_SMEM, s>>>(
-                h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2), h->table, h->bricks, counters(h), kp, h->masks,
-                h->err);
-        };
-        if (kp.dims == 2) {
-            if (fused) launch(k_force_cells<2, true, false>);
-            else launch(k_force_cells<2, false, false>);
-        } else {
-            if (fused) launch(k_force_cells<3, true, false>);
-            else launch(k_force_cells<3, false, false>);
-        }
-        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
-        return GBSPH_OK;
-    }
     auto launch = [&](auto kern) {
         kern<<<h->force_blocks, BRICK_THREADS, FORCE_SMEM, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2),
                                                                 h->table, h->bricks, counters(h), kp, h->nbr,
@@ -608,17 +579,6 @@ int setup_kernels(H* h) {
     h->dens_blocks = std::max(1, nb) * sms;
     GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true, false>, BRICK_THREADS, FORCE_SMEM));
     h->force_blocks = std::max(1, nb) * sms;
-    const int dcs = (int)DENSITY_CELLS_SMEM, fcs = (int)FORCE_CELLS_SMEM;
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_cells<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_density_cells<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_cells<3, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_cells<3, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_cells<2, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaFuncSetAttribute(k_force_cells<2, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, fcs));
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_density_cells<3, false>, BRICK_THREADS, DENSITY_CELLS_SMEM));
-    h->dens_cells_blocks = std::max(1, nb) * sms;
-    GBSPH_CUDA_TRY(&h->last_error, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_cells<3, true, false>, BRICK_THREADS, FORCE_CELLS_SMEM));
-    h->force_cells_blocks = std::max(1, nb) * sms;
     return GBSPH_OK;
 }
 
@@ -829,7 +789,6 @@ GBSPH_API int gbsph_fluid3d_set_option(gbsph_fluid3d_t h, int option, int value)
             h->opt_bw = value;
             break;
         case GBSPH_OPT_PROFILE: h->opt_profile = value ? 1 : 0; break;
-        case GBSPH_OPT_NEIGHBOUR_LISTS: h->opt_lists = value ? 1 : 0; break;
         default: return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown option");
     }
     invalidate_graph(h);

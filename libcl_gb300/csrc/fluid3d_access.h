@@ -2,7 +2,7 @@
 // fluid handle; implemented in fluid3d.cu.
 #pragma once
 
-#include "cell_kernels.cuh"
+#include "fluid3d_kernels.cuh"
 
 namespace gbsph {
 
