@@ -293,11 +293,13 @@ def _time_steps(fn, steps: int, stream) -> float:
     return e0.elapsed_time(e1)
 
 
-def extra_batched(stream, steps: int = 10) -> dict:
-    """256 independent scenes (log-uniform 4,096-262,144 particles): one batched step vs the
-    plain step looped over the same scenes."""
+def extra_batched(stream, steps: int = 200) -> dict:
+    """256 independent scenes (log-uniform 4,096-262,144 particles, 17.3M in all): `steps`
+    batched steps in the configuration the autotuner chose (step form, brick width, sort digit
+    width, sort tile), the other step form beside it, and the plain step looped over the same
+    scenes for as many steps."""
     import torch
-    from libcl_gb300 import BUF_FORCE, BUF_POSITION, BUF_VELOCITY, Batch3D, Fluid3D
+    from libcl_gb300 import BUF_FORCE, BUF_POSITION, BUF_VELOCITY, OPT_PERSISTENT, Batch3D, Fluid3D
     from libcl_gb300.scenes import batched_ensemble
     b = batched_ensemble()
     bt = Batch3D()
@@ -305,10 +307,17 @@ def extra_batched(stream, steps: int = 10) -> dict:
     bt.buffer(BUF_POSITION).copy_(torch.from_numpy(b.pos))
     bt.buffer(BUF_VELOCITY).zero_()
     bt.buffer(BUF_FORCE).zero_()
-    best_w = bt.autotune(stream)
+    bt.autotune(stream)
+    cfg = bt.config()
     for _ in range(3):
         bt.compute(stream)
     t_b = _time_steps(lambda: bt.compute(stream), steps, stream)
+    assert bt.sync_status() == 0
+    # the other step form, same configuration otherwise, from the state reached
+    bt.set_option(OPT_PERSISTENT, 1 - cfg["persistent"])
+    for _ in range(3):
+        bt.compute(stream)
+    t_o = _time_steps(lambda: bt.compute(stream), steps, stream)
     assert bt.sync_status() == 0
     del bt
     fluids = []
@@ -319,12 +328,18 @@ def extra_batched(stream, steps: int = 10) -> dict:
     for _ in range(3):
         for f in fluids:
             f.compute(stream)
-    t_l = _time_steps(lambda: [f.compute(stream) for f in fluids], max(2, steps // 2), stream)
-    looped = b.n * max(2, steps // 2) / (t_l * 1e-3)
+    t_l = _time_steps(lambda: [f.compute(stream) for f in fluids], steps, stream)
+    looped = b.n * steps / (t_l * 1e-3)
     batched = b.n * steps / (t_b * 1e-3)
-    return {"scenes": len(b.descs), "particles": b.n, "brick_width": best_w,
+    forms = {cfg["persistent"]: t_b / steps, 1 - cfg["persistent"]: t_o / steps}
+    return {"scenes": len(b.descs), "particles": b.n, "steps": steps,
+            "config": {"step_form": "persistent" if cfg["persistent"] else "staged graph",
+                       "brick_width": cfg["brick_width"], "radix_bits": cfg["radix_bits"],
+                       "sort_tile_keys": 256 * cfg["sort_tile_items"]},
             "batched_particle_steps_per_s": batched, "looped_particle_steps_per_s": looped,
-            "speedup": batched / looped, "batched_ms_per_step": t_b / steps}
+            "speedup": batched / looped, "batched_ms_per_step": t_b / steps,
+            "staged_graph_ms_per_step": forms[0], "persistent_ms_per_step": forms[1],
+            "looped_ms_per_step": t_l / steps}
 
 
 def extra_sort(stream) -> dict:

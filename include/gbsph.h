@@ -38,7 +38,8 @@ enum {
     GBSPH_ERR_TOO_LARGE = -3,       /* element count beyond what the kernels address */
     GBSPH_ERR_BIT_RANGE = -4,       /* (end_bit - start_bit) not a multiple of 4, or outside [0,32] */
     GBSPH_ERR_CUDA = -5,            /* a CUDA runtime call failed; see *_last_error() */
-    GBSPH_ERR_DEVICE_TIMEOUT = -6,  /* a bounded device-side wait (look-back, mbarrier) gave up */
+    GBSPH_ERR_DEVICE_TIMEOUT = -6,  /* a bounded device-side wait (look-back, mbarrier, grid
+                                       barrier) gave up */
     GBSPH_ERR_NOT_COMPILED = -7,    /* compute() before compile() */
     GBSPH_ERR_OUT_OF_MEMORY = -8,
     GBSPH_ERR_DEVICE_RANGE = -9,    /* a key/cell index fell outside its table on the device */
@@ -57,9 +58,11 @@ GBSPH_API const char* gbsph_status_string(int status);
  *              delivers;
  *   which = 2: the pass of which = 0 run inside the allocation-free sort's static array: it
  *              returns without synchronising, and gbsph_radix_sort_noalloc_status reports
- *              the timeout.
+ *              the timeout;
+ *   which = 3: two CTAs at the persistent batch step's grid-wide barrier, counting on a
+ *              third CTA that does not exist.
  * Each wait gives up after about one second, sets its device error bit and the kernel ends;
- * for which = 0 and 1 the call synchronises `stream` and returns GBSPH_ERR_DEVICE_TIMEOUT if
+ * for which = 0, 1 and 3 the call synchronises `stream` and returns GBSPH_ERR_DEVICE_TIMEOUT if
  * that happened (and the context stays usable), GBSPH_OK if the wait somehow completed, or
  * an argument/CUDA error. */
 GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream);
@@ -200,9 +203,17 @@ enum {
     GBSPH_OPT_FUSED = 0,      /* 1 (default): fused kernels; 0: one kernel per reference stage */
     GBSPH_OPT_CUDA_GRAPH = 1, /* 1 (default): replay the step as a captured CUDA graph */
     GBSPH_OPT_BRICK_WIDTH = 2, /* LINEAR_GRID neighbour bricks: cells per brick along x (1..16) */
-    GBSPH_OPT_PROFILE = 3      /* 1: compute() runs eagerly and records a CUDA event pair per
+    GBSPH_OPT_PROFILE = 3,     /* 1: compute() runs eagerly and records a CUDA event pair per
                                   stage (the reference's CL_QUEUE_PROFILING_ENABLE events,
                                   libCL/oclDevice.cpp:31, libCL/oclKernel.cpp:162-202) */
+    GBSPH_OPT_RADIX_BITS = 4,  /* batches: key bits sorted per radix pass (5..8, default 8; at
+                                  most four passes over the batch's key width) */
+    GBSPH_OPT_SORT_TILE = 5,   /* batches: keys per thread of a sort tile (8 or 16; 0, the
+                                  default: 8 up to 2^21 keys, else 16) */
+    GBSPH_OPT_PERSISTENT = 6   /* batches: 1 = the whole step (hash, sort passes, cell bounds,
+                                  density, forces and integration) as one cooperative kernel
+                                  whose CTAs stay resident and meet at grid-wide barriers;
+                                  0 (default) = one kernel per stage, replayed as a graph */
 };
 
 typedef struct gbsph_fluid3d_s* gbsph_fluid3d_t;
@@ -316,12 +327,19 @@ GBSPH_API int gbsph_batch3d_set_scenes(gbsph_batch3d_t h, const gbsph_fluid3d_pa
 GBSPH_API void* gbsph_batch3d_get_buffer(gbsph_batch3d_t h, int which, size_t* count);
 /* First particle and particle count of scene `s`. */
 GBSPH_API int gbsph_batch3d_scene_range(gbsph_batch3d_t h, int s, size_t* first, size_t* count);
-/* GBSPH_OPT_CUDA_GRAPH, GBSPH_OPT_BRICK_WIDTH. */
+/* GBSPH_OPT_CUDA_GRAPH, GBSPH_OPT_BRICK_WIDTH, GBSPH_OPT_RADIX_BITS, GBSPH_OPT_SORT_TILE,
+ * GBSPH_OPT_PERSISTENT. A digit width that needs more than four passes over the batch's
+ * keys is refused by compute() (GBSPH_ERR_ARGUMENT). */
 GBSPH_API int gbsph_batch3d_set_option(gbsph_batch3d_t h, int option, int value);
+/* Current value of one of the options above. */
+GBSPH_API int gbsph_batch3d_get_option(gbsph_batch3d_t h, int option, int* value);
 /* One step of every scene, asynchronous on `stream`. */
 GBSPH_API int gbsph_batch3d_compute(gbsph_batch3d_t h, void* stream);
-/* Times the step for brick widths 4, 8 and 16 on the current state (which is saved and
- * restored), keeps the fastest and returns it through best_width. Synchronises `stream`. */
+/* Times the step on the current state (which is saved and restored) for every combination
+ * of brick width (4, 8, 16), sort digit width (6, 7, 8 bits, where four passes cover the
+ * keys), sort tile (8 or 16 keys per thread) and step form (staged graph or persistent
+ * kernel), keeps the fastest and returns its brick width through best_width (the others
+ * through gbsph_batch3d_get_option). Synchronises `stream`. */
 GBSPH_API int gbsph_batch3d_autotune(gbsph_batch3d_t h, void* stream, int* best_width);
 GBSPH_API int gbsph_batch3d_sync_status(gbsph_batch3d_t h, void* stream);
 GBSPH_API const char* gbsph_batch3d_last_error(gbsph_batch3d_t h);

@@ -35,7 +35,7 @@ KEY_LINEAR_GRID = 1
 BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY, BUF_INDEX, BUF_CELL, BUF_PARAMS = range(8)
 (STAGE_HASH, STAGE_SORT, STAGE_REORDER, STAGE_BOUNDS, STAGE_DENSITY, STAGE_FORCES, STAGE_CLIP_BOX,
  STAGE_INTEGRATE_FORCE, STAGE_GRAVITY, STAGE_INTEGRATE_VELOCITY) = range(10)
-OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE = range(4)
+OPT_FUSED, OPT_CUDA_GRAPH, OPT_BRICK_WIDTH, OPT_PROFILE, OPT_RADIX_BITS, OPT_SORT_TILE, OPT_PERSISTENT = range(7)
 STAGE_TIME_NAMES = ("front_end", "sort", "bounds", "density", "forces")
 
 REF_BUCKETS = 262144  # cBucketCount, libCL/phys/oclFluid3D.cpp:17
@@ -112,6 +112,7 @@ SIGNATURES = {
     "gbsph_batch3d_get_buffer": (_P, [_P, _I, C.POINTER(_SZ)]),
     "gbsph_batch3d_scene_range": (_I, [_P, _I, C.POINTER(_SZ), C.POINTER(_SZ)]),
     "gbsph_batch3d_set_option": (_I, [_P, _I, _I]),
+    "gbsph_batch3d_get_option": (_I, [_P, _I, C.POINTER(_I)]),
     "gbsph_batch3d_compute": (_I, [_P, _P]),
     "gbsph_batch3d_autotune": (_I, [_P, _P, C.POINTER(_I)]),
     "gbsph_batch3d_sync_status": (_I, [_P, _P]),
@@ -622,6 +623,19 @@ class Batch3D:
 
     def set_option(self, option: int, value: int) -> None:
         self._check(self._lib.gbsph_batch3d_set_option(self._h, option, value))
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int()
+        self._check(self._lib.gbsph_batch3d_get_option(self._h, option, C.byref(v)))
+        return v.value
+
+    def config(self) -> dict:
+        """The step's current launch configuration (what autotune() chose)."""
+        return {"brick_width": self.get_option(OPT_BRICK_WIDTH),
+                "radix_bits": self.get_option(OPT_RADIX_BITS),
+                "sort_tile_items": self.get_option(OPT_SORT_TILE),
+                "cuda_graph": self.get_option(OPT_CUDA_GRAPH),
+                "persistent": self.get_option(OPT_PERSISTENT)}
 
     def compute(self, stream=None) -> None:
         self._check(self._lib.gbsph_batch3d_compute(self._h, _stream(stream)))

@@ -5,8 +5,9 @@
 // hash, one sort, one bounds pass, one density and one force launch advance every scene. The
 // brick kernels find a brick's scene by binary search over the scene table and take its gas
 // constant, viscosity, box and grid from there; particles of different scenes are never in
-// the same brick, so scenes cannot interact. The step is replayed as one CUDA graph; an
-// autotuner picks the brick width.
+// the same brick, so scenes cannot interact. The step is replayed as one CUDA graph of one
+// kernel per stage, or runs as one persistent cooperative kernel (k_batch_step); an
+// autotuner picks the form, the brick width, the sort's digit width and its tile size.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -14,8 +15,116 @@
 #include <vector>
 
 #include "fluid3d_kernels.cuh"
+#include "grid_sync.cuh"
+#include "onesweep.cuh"
 
 using namespace gbsph;
+
+namespace {
+
+// ---- the persistent step ------------------------------------------------------------------
+
+// Where k_batch_step keeps its grid barrier's words: offset in the sort scratch's caller
+// counters (zeroed with the scratch before each step), on a cache line of their own.
+constexpr uint32_t GRID_SYNC_WORD = 32;
+
+struct BatchStepArgs {
+    float4 *pos, *vel, *force, *spos, *svel;
+    uint32_t *keys_a, *keys_b, *keys_c, *vals_a, *vals_b, *index, *bricks;
+    uint16_t* nbr;
+    uint64_t* nbr_meta;
+    uint2* table;
+    uint32_t* scratch;
+    uint32_t* err;
+    int clear;  // reset the previous step's table entries (keys_c) in the hash phase
+};
+
+// Dynamic shared memory of k_batch_step: each phase carves its own layout out of one buffer
+// (the force phase's is the largest).
+constexpr size_t STEP_SMEM = FORCE_SMEM;
+static_assert(DENSITY_SMEM + sizeof(SubListCounts) <= STEP_SMEM, "density phase layout");
+static_assert(onesweep_smem_words(SORT_ITEMS) * 4 <= STEP_SMEM, "sort phase layout");
+static_assert(SORT_MAX_PASSES * SORT_RADIX * 4 <= STEP_SMEM, "hash phase layout");
+
+// One step of every scene in one launch: hash + digit histograms, the radix-sort passes (the
+// last gathers the sorted state), cell bounds + occupied bricks, density, forces +
+// integration, with a grid-wide barrier between phases. Every phase takes its work from an
+// atomic queue (sort tiles, brick ids) or strides over the grid, so the grid is whatever is
+// resident: occupancy x SMs. Data written by one phase and read by a later one is read
+// through L2 (ld_phase<true>) or by bulk copies after the barrier's proxy fence.
+template <int ITEMS>
+__global__ void __launch_bounds__(BRICK_THREADS, 3) k_batch_step(BatchStepArgs a, KParams kp) {
+    extern __shared__ float4 s_dyn[];
+    __shared__ BrickShared S;
+    __shared__ LaneMap L;
+    __shared__ uint32_t s_flag;
+    uint32_t* words = reinterpret_cast<uint32_t*>(s_dyn);
+    uint32_t* counters = a.scratch + SORT_USER_COUNTER_OFFSET / 4;
+    GridSync gs{counters + GRID_SYNC_WORD, a.err, 0u, gridDim.x};
+
+    if (a.clear) hash_batch_run<true>(words, a.pos, kp, a.keys_a, a.scratch, a.keys_c, a.table);
+    else hash_batch_run<false>(words, a.pos, kp, a.keys_a, a.scratch, nullptr, nullptr);
+    if (!gs.sync(&s_flag)) return;
+
+    const int P = sort_passes(0, kp.end_bit, kp.digit_bits);
+    const uint32_t tiles = sort_tiles(kp.n, SORT_THREADS * ITEMS);
+    const OnesweepSmem sm = onesweep_smem<ITEMS>(words);
+    SortGather g;
+    g.n_gather = 2;
+    g.src[0] = a.pos;
+    g.src[1] = a.vel;
+    g.dst[0] = a.spos;
+    g.dst[1] = a.svel;
+    const uint32_t* kin = a.keys_a;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < P; ++p) {
+        const bool last = p == P - 1;
+        uint32_t* kout = last ? a.keys_c : ((p & 1) ? a.keys_a : a.keys_b);
+        uint32_t* vout = last ? a.index : ((p & 1) ? a.vals_a : a.vals_b);
+        const int shift = p * kp.digit_bits, bits = min(kp.digit_bits, kp.end_bit - shift);
+        if (p == 0 && last) {
+            while (onesweep_tile<true, 2, ITEMS, true>(sm, kin, vin, kout, vout, kp.n, shift, bits, p, tiles, a.scratch,
+                                                       a.err, g)) {
+            }
+        } else if (p == 0) {
+            while (onesweep_tile<true, 0, ITEMS, true>(sm, kin, vin, kout, vout, kp.n, shift, bits, p, tiles, a.scratch,
+                                                       a.err, g)) {
+            }
+        } else if (last) {
+            while (onesweep_tile<false, 2, ITEMS, true>(sm, kin, vin, kout, vout, kp.n, shift, bits, p, tiles,
+                                                        a.scratch, a.err, g)) {
+            }
+        } else {
+            while (onesweep_tile<false, 0, ITEMS, true>(sm, kin, vin, kout, vout, kp.n, shift, bits, p, tiles,
+                                                        a.scratch, a.err, g)) {
+            }
+        }
+        if (!gs.sync(&s_flag)) return;
+        kin = kout;
+        vin = vout;
+    }
+
+    const uint32_t btiles = (kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE;
+    for (uint32_t tile = blockIdx.x; tile < btiles; tile += gridDim.x)
+        bounds_tile<true>(a.keys_c, kp, a.table, a.bricks, counters, a.err,
+                          [&](uint32_t k) { return batch_brick_of(kp, k); }, tile);
+    if (!gs.sync(&s_flag)) return;
+
+    SubListCounts& wcnt = *reinterpret_cast<SubListCounts*>(reinterpret_cast<char*>(s_dyn) + DENSITY_SMEM);
+    const bool ok = density_brick_run<3, true>(s_dyn, S, L, wcnt, a.spos, a.svel, a.table, a.bricks, counters, kp,
+                                               a.nbr, a.nbr_meta, a.err);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (ok) mbar_inval(reinterpret_cast<uint64_t*>(&S.bar));  // the force phase initialises it again
+        else gs.abort();
+    }
+    if (!gs.sync(&s_flag)) return;
+
+    force_brick_run<3, true, true, true>(s_dyn, S, L, a.spos, a.svel, a.index, a.pos, a.vel, a.force, a.table, a.bricks,
+                                         counters, kp, a.nbr, a.nbr_meta, a.err);
+}
+
+}  // namespace
 
 struct gbsph_batch3d_s {
     int device = 0;
@@ -35,6 +144,10 @@ struct gbsph_batch3d_s {
     void* scratch = nullptr;
     uint32_t* err = nullptr;
     int bw = 8, use_graph = 1, sdev_bw = -1;
+    int digit_bits = SORT_RADIX_BITS;  // bits per sort pass (5 to 8)
+    int sort_items = 0;                // keys per thread of a sort tile (8 or 16; 0: by key count)
+    int persistent = 0;                // 1: the step is one cooperative k_batch_step launch
+    int step_blocks[2] = {0, 0};       // resident k_batch_step CTAs (8 and 16 keys per thread)
     int dens_blocks = 0, force_blocks = 0;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -115,6 +228,7 @@ KParams make_kp(const B* h) {
     k.key_mode = GBSPH_KEY_LINEAR_GRID;
     k.dims = 3;
     k.end_bit = bits_for_b(h->cells);
+    k.digit_bits = h->digit_bits;
     k.bw = h->bw;
     k.n = (uint32_t)h->n;
     k.table_cells = (uint32_t)h->cells;
@@ -133,7 +247,7 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     const bool clear = h->table_clean;
     if (!clear) GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->cells * sizeof(uint2), s));
     h->table_clean = false;
-    GBSPH_CUDA_TRY(&h->last_error, onesweep_prepare(h->scratch, kp.n, sort_passes(0, kp.end_bit), s));
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_prepare(h->scratch, kp.n, sort_passes(0, kp.end_bit, kp.digit_bits), s));
     const int blocks = std::max(1, std::min((int)((kp.n + 255) / 256), num_sms() * 8));
     if (clear)
         k_hash_batch<true><<<blocks, 256, 0, s>>>(h->pos, kp, h->keys_a, (uint32_t*)h->scratch, h->keys_c, h->table);
@@ -150,6 +264,8 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     a.tmp_vals[1] = h->vals_a;
     a.n = kp.n;
     a.end_bit = kp.end_bit;
+    a.digit_bits = kp.digit_bits;
+    a.items = h->sort_items;
     a.scratch = h->scratch;
     a.err = h->err;
     a.gather.n_gather = 2;
@@ -170,9 +286,56 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
     return GBSPH_OK;
 }
 
+int sort_items_of(const B* h) { return h->sort_items ? h->sort_items : sort_items_for((uint32_t)h->n); }
+
+// The persistent form: table reset (when needed) and scratch clear, then one cooperative
+// launch. It runs eagerly (three stream operations per step).
+int enqueue_persistent(B* h, const KParams& kp, cudaStream_t s) {
+    const bool clear = h->table_clean;
+    if (!clear) GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->cells * sizeof(uint2), s));
+    h->table_clean = false;
+    GBSPH_CUDA_TRY(&h->last_error, onesweep_prepare(h->scratch, kp.n, sort_passes(0, kp.end_bit, kp.digit_bits), s));
+    BatchStepArgs a;
+    a.pos = h->pos;
+    a.vel = h->vel;
+    a.force = h->force;
+    a.spos = h->spos;
+    a.svel = h->svel;
+    a.keys_a = h->keys_a;
+    a.keys_b = h->keys_b;
+    a.keys_c = h->keys_c;
+    a.vals_a = h->vals_a;
+    a.vals_b = h->vals_b;
+    a.index = h->index;
+    a.bricks = h->bricks;
+    a.nbr = h->nbr;
+    a.nbr_meta = h->nbr_meta;
+    a.table = h->table;
+    a.scratch = (uint32_t*)h->scratch;
+    a.err = h->err;
+    a.clear = clear ? 1 : 0;
+    KParams k = kp;
+    void* args[2] = {&a, &k};
+    const bool big = sort_items_of(h) == 16;
+    const void* fn = big ? (const void*)k_batch_step<16> : (const void*)k_batch_step<8>;
+    GBSPH_CUDA_TRY(&h->last_error, cudaLaunchCooperativeKernel(fn, dim3(h->step_blocks[big ? 1 : 0]), dim3(BRICK_THREADS),
+                                                               args, STEP_SMEM, s));
+    h->table_clean = true;
+    return GBSPH_OK;
+}
+
 int bcompute(B* h, cudaStream_t s, bool allow_graph) {
     BRC(upload_scenes(h));
     const KParams kp = make_kp(h);
+    if (sort_passes(0, kp.end_bit, kp.digit_bits) > SORT_MAX_PASSES)
+        return fail(&h->last_error, GBSPH_ERR_ARGUMENT,
+                    std::to_string(kp.digit_bits) + "-bit digits need more than four passes over " +
+                        std::to_string(kp.end_bit) + "-bit keys");
+    if (h->persistent) {
+        const int rc = enqueue_persistent(h, kp, s);
+        if (rc) h->table_clean = false;
+        return rc;
+    }
     if (!h->use_graph || !allow_graph || !h->table_clean) {
         const int rc = enqueue_batch(h, kp, s);
         if (rc) h->table_clean = false;
@@ -233,6 +396,13 @@ GBSPH_API int gbsph_batch3d_create(gbsph_batch3d_t* out) {
         if (!rc && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_brick<3, true, true>, BRICK_THREADS, FORCE_SMEM))
             rc = GBSPH_ERR_CUDA;
         h->force_blocks = std::max(1, nb) * sms;
+        const void* steps[2] = {(const void*)k_batch_step<8>, (const void*)k_batch_step<16>};
+        for (int i = 0; i < 2 && !rc; i++) {
+            if (cudaFuncSetAttribute(steps[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)STEP_SMEM) ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, steps[i], BRICK_THREADS, STEP_SMEM))
+                rc = GBSPH_ERR_CUDA;
+            h->step_blocks[i] = nb * sms;  // 0: the persistent form cannot run here
+        }
     }
     if (rc) {
         cudaGetLastError();
@@ -357,10 +527,34 @@ GBSPH_API int gbsph_batch3d_set_option(gbsph_batch3d_t h, int option, int value)
     } else if (option == GBSPH_OPT_BRICK_WIDTH) {
         if (value < 1 || value > BRICK_W_MAX) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "brick width must be in [1, 16]");
         h->bw = value;
+    } else if (option == GBSPH_OPT_RADIX_BITS) {
+        if (value < 5 || value > SORT_RADIX_BITS) return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "radix bits must be in [5, 8]");
+        h->digit_bits = value;
+    } else if (option == GBSPH_OPT_SORT_TILE) {
+        if (value != 0 && value != 8 && value != 16)
+            return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "sort tile must be 0, 8 or 16 keys per thread");
+        h->sort_items = value;
+    } else if (option == GBSPH_OPT_PERSISTENT) {
+        if (value && (h->step_blocks[0] == 0 || h->step_blocks[1] == 0))
+            return fail(&h->last_error, GBSPH_ERR_STATE, "the persistent step does not fit on this device");
+        h->persistent = value ? 1 : 0;
     } else {
         return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown option");
     }
     binvalidate(h);
+    return GBSPH_OK;
+}
+
+GBSPH_API int gbsph_batch3d_get_option(gbsph_batch3d_t h, int option, int* value) {
+    if (!h || !value) return GBSPH_ERR_ARGUMENT;
+    switch (option) {
+        case GBSPH_OPT_CUDA_GRAPH: *value = h->use_graph; break;
+        case GBSPH_OPT_BRICK_WIDTH: *value = h->bw; break;
+        case GBSPH_OPT_RADIX_BITS: *value = h->digit_bits; break;
+        case GBSPH_OPT_SORT_TILE: *value = h->sort_items; break;
+        case GBSPH_OPT_PERSISTENT: *value = h->persistent; break;
+        default: return fail(&h->last_error, GBSPH_ERR_ARGUMENT, "unknown option");
+    }
     return GBSPH_OK;
 }
 
@@ -383,11 +577,20 @@ GBSPH_API int gbsph_batch3d_autotune(gbsph_batch3d_t h, void* stream, int* best_
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    const int widths[3] = {4, 8, 16};
+    // every combination of brick width x digit width x sort tile x step form
+    const int widths[3] = {4, 8, 16}, digits[3] = {6, 7, 8}, items[2] = {8, 16};
+    const int forms = (h->step_blocks[0] && h->step_blocks[1]) ? 2 : 1;
+    const int end_bit = bits_for_b(h->cells);
     float best = 1e30f;
-    int best_w = h->bw, rc = GBSPH_OK;
-    for (int w : widths) {
+    int best_w = h->bw, best_d = h->digit_bits, best_i = h->sort_items, best_p = h->persistent, rc = GBSPH_OK;
+    for (int c = 0; c < 3 * 3 * 2 * forms && !rc; c++) {
+        const int w = widths[c / (3 * 2 * forms)], d = digits[(c / (2 * forms)) % 3], it = items[(c / forms) % 2],
+                  pf = c % forms;
+        if (sort_passes(0, end_bit, d) > SORT_MAX_PASSES) continue;
         h->bw = w;
+        h->digit_bits = d;
+        h->sort_items = it;
+        h->persistent = pf;
         binvalidate(h);
         for (int i = 0; i < 2 && !rc; i++) rc = bcompute(h, s, true);  // eager + capture
         if (!rc) cudaEventRecord(e0, s);
@@ -400,6 +603,9 @@ GBSPH_API int gbsph_batch3d_autotune(gbsph_batch3d_t h, void* stream, int* best_
         if (ms < best) {
             best = ms;
             best_w = w;
+            best_d = d;
+            best_i = it;
+            best_p = pf;
         }
         cudaMemcpyAsync(h->pos, saved, 3 * st, cudaMemcpyDeviceToDevice, s);
     }
@@ -408,6 +614,9 @@ GBSPH_API int gbsph_batch3d_autotune(gbsph_batch3d_t h, void* stream, int* best_
     cudaEventDestroy(e1);
     cudaFree(saved);
     h->bw = best_w;
+    h->digit_bits = best_d;
+    h->sort_items = best_i;
+    h->persistent = best_p;
     h->table_clean = false;
     binvalidate(h);
     if (best_width) *best_width = best_w;

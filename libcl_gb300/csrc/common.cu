@@ -25,7 +25,7 @@ int fail(std::string* last_error, int status, const std::string& msg) {
 
 int dev_err_to_status(uint32_t bits) {
     if (bits == 0) return GBSPH_OK;
-    if (bits & (DEV_ERR_LOOKBACK_TIMEOUT | DEV_ERR_MBAR_TIMEOUT)) return GBSPH_ERR_DEVICE_TIMEOUT;
+    if (bits & (DEV_ERR_LOOKBACK_TIMEOUT | DEV_ERR_MBAR_TIMEOUT | DEV_ERR_GRID_TIMEOUT)) return GBSPH_ERR_DEVICE_TIMEOUT;
     if (bits & DEV_ERR_KEY_RANGE) return GBSPH_ERR_DEVICE_RANGE;
     return GBSPH_ERR_STATE;
 }

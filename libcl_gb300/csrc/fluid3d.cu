@@ -210,6 +210,7 @@ KParams make_kparams(const H* h) {
         k.table_cells = REF_BUCKETS;
         k.end_bit = 18;  // keys < 2^18; the reference sorts bits [0, 24) of the same keys
     }
+    k.digit_bits = SORT_RADIX_BITS;
     k.bw = h->opt_bw;
     k.bxn = k.nx > 0 ? (k.nx + k.bw - 1) / k.bw : 0;
     k.n = (uint32_t)h->n;

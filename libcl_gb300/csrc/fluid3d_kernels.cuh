@@ -44,7 +44,8 @@ struct KParams {
     float4 gravity, box_min, box_max, origin;
     int nx, ny, nz;
     int key_mode, dims;
-    int end_bit;  // sort bits [0, end_bit)
+    int end_bit;     // sort bits [0, end_bit)
+    int digit_bits;  // sort digit width (bits per pass)
     int bw, bxn;  // brick width (cells) and bricks per x row
     uint32_t n;
     uint32_t table_cells;
@@ -122,13 +123,13 @@ __global__ void __launch_bounds__(256) k_hash(const float4* __restrict__ pos, KP
     __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
     for (int i = threadIdx.x; i < SORT_MAX_PASSES * SORT_RADIX; i += blockDim.x) s_h[i] = 0;
     __syncthreads();
-    const int passes = sort_passes(0, kp.end_bit);
+    const int passes = sort_passes(0, kp.end_bit, kp.digit_bits);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kp.n; i += gridDim.x * blockDim.x) {
         const uint32_t k = particle_key(kp, pos[i]);
         keys[i] = k;
         for (int p = 0; p < passes; ++p) {
-            const int shift = p * SORT_RADIX_BITS;
-            const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
+            const int shift = p * kp.digit_bits;
+            const int bits = min(kp.digit_bits, kp.end_bit - shift);
             atomicAdd(&s_h[p * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
         }
         if (CLEAR) {
@@ -162,28 +163,30 @@ static __global__ void k_reorder(const uint32_t* __restrict__ index, const float
 constexpr uint32_t BOUNDS_ITEMS = 4;
 constexpr uint32_t BOUNDS_TILE = 256 * BOUNDS_ITEMS;
 
-template <class BrickOf>
+// Tile `tile` of the keys; COH: the keys were written earlier in the same launch.
+template <bool COH = false, class BrickOf>
 __device__ __forceinline__ void bounds_tile(const uint32_t* __restrict__ keys, const KParams& kp,
                                             uint2* __restrict__ table, uint32_t* __restrict__ bricks,
-                                            uint32_t* __restrict__ n_bricks, uint32_t* err, BrickOf brick_of) {
+                                            uint32_t* __restrict__ n_bricks, uint32_t* err, BrickOf brick_of,
+                                            uint32_t tile) {
     __shared__ uint32_t s_cnt, s_base;
     if (threadIdx.x == 0) s_cnt = 0;
     __syncthreads();
     uint32_t bid[BOUNDS_ITEMS], rank[BOUNDS_ITEMS];
-    const uint32_t i0 = blockIdx.x * BOUNDS_TILE + threadIdx.x;
+    const uint32_t i0 = tile * BOUNDS_TILE + threadIdx.x;
 #pragma unroll
     for (uint32_t it = 0; it < BOUNDS_ITEMS; ++it) {
         const uint32_t i = i0 + it * blockDim.x;
         rank[it] = EMPTY;
         bid[it] = 0;
         if (i >= kp.n) continue;
-        const uint32_t k = keys[i];
+        const uint32_t k = ld_phase<COH>(keys + i);
         if (k >= kp.table_cells) {
             atomicOr(err, DEV_ERR_KEY_RANGE);
             continue;
         }
-        const uint32_t prev = i > 0 ? keys[i - 1] : EMPTY;
-        const uint32_t next = i + 1 < kp.n ? keys[i + 1] : EMPTY;
+        const uint32_t prev = i > 0 ? ld_phase<COH>(keys + i - 1) : EMPTY;
+        const uint32_t next = i + 1 < kp.n ? ld_phase<COH>(keys + i + 1) : EMPTY;
         if (k != prev) table[k].x = i;
         if (k != next) table[k].y = i + 1;
         bid[it] = brick_of(k);
@@ -203,19 +206,19 @@ static __global__ void __launch_bounds__(256) k_bounds_linear(const uint32_t* __
                                                               uint32_t* __restrict__ n_bricks, uint32_t* err) {
     const uint32_t nx = (uint32_t)kp.nx, bw = (uint32_t)kp.bw, bxn = (uint32_t)kp.bxn;
     bounds_tile(keys, kp, table, bricks, n_bricks, err,
-                [=](uint32_t k) { return (k % nx) / bw + bxn * (k / nx); });
+                [=](uint32_t k) { return (k % nx) / bw + bxn * (k / nx); }, blockIdx.x);
 }
 
 // Batch version of k_hash: each particle keys into its own scene's grid; the key is the
-// scene's cell offset plus the local linear key.
+// scene's cell offset plus the local linear key. The body takes the block's histogram
+// buffer (SORT_MAX_PASSES * SORT_RADIX words of shared memory) from the caller.
 template <bool CLEAR>
-__global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ pos, KParams kp,
-                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
-                                                    const uint32_t* __restrict__ prev_keys, uint2* __restrict__ table) {
-    __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
+__device__ __forceinline__ void hash_batch_run(uint32_t* s_h, const float4* __restrict__ pos, const KParams& kp,
+                                               uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                                               const uint32_t* __restrict__ prev_keys, uint2* __restrict__ table) {
     for (int i = threadIdx.x; i < SORT_MAX_PASSES * SORT_RADIX; i += blockDim.x) s_h[i] = 0;
     __syncthreads();
-    const int passes = sort_passes(0, kp.end_bit);
+    const int passes = sort_passes(0, kp.end_bit, kp.digit_bits);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kp.n; i += gridDim.x * blockDim.x) {
         const SceneDev& d = kp.scenes[scene_of<0>(kp.scenes, kp.n_scenes, i)];
         const float4 p = pos[i];
@@ -226,8 +229,8 @@ __global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ p
                            (uint32_t)d.nx * ((uint32_t)clampi(gy, 0, d.ny - 1) + (uint32_t)d.ny * (uint32_t)clampi(gz, 0, d.nz - 1));
         keys[i] = k;
         for (int q = 0; q < passes; ++q) {
-            const int shift = q * SORT_RADIX_BITS;
-            const int bits = min(SORT_RADIX_BITS, kp.end_bit - shift);
+            const int shift = q * kp.digit_bits;
+            const int bits = min(kp.digit_bits, kp.end_bit - shift);
             atomicAdd(&s_h[q * SORT_RADIX + ((k >> shift) & ((1u << bits) - 1u))], 1u);
         }
         if (CLEAR) {
@@ -238,6 +241,15 @@ __global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ p
     __syncthreads();
     for (int i = threadIdx.x; i < passes * SORT_RADIX; i += blockDim.x)
         if (s_h[i]) atomicAdd(&hist[i], s_h[i]);
+    __syncthreads();  // s_h is free for the caller
+}
+
+template <bool CLEAR>
+__global__ void __launch_bounds__(256) k_hash_batch(const float4* __restrict__ pos, KParams kp,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                                                    const uint32_t* __restrict__ prev_keys, uint2* __restrict__ table) {
+    __shared__ uint32_t s_h[SORT_MAX_PASSES * SORT_RADIX];
+    hash_batch_run<CLEAR>(s_h, pos, kp, keys, hist, prev_keys, table);
 }
 
 __device__ __forceinline__ uint32_t batch_brick_of(const KParams& kp, uint32_t k) {
@@ -250,7 +262,7 @@ __device__ __forceinline__ uint32_t batch_brick_of(const KParams& kp, uint32_t k
 static __global__ void __launch_bounds__(256) k_bounds_batch(const uint32_t* __restrict__ keys, KParams kp,
                                                              uint2* __restrict__ table, uint32_t* __restrict__ bricks,
                                                              uint32_t* __restrict__ n_bricks, uint32_t* err) {
-    bounds_tile(keys, kp, table, bricks, n_bricks, err, [&](uint32_t k) { return batch_brick_of(kp, k); });
+    bounds_tile(keys, kp, table, bricks, n_bricks, err, [&](uint32_t k) { return batch_brick_of(kp, k); }, blockIdx.x);
 }
 
 // Splits the interleaved table into two arrays (for inspection through the ABI).
@@ -344,9 +356,10 @@ __global__ void __launch_bounds__(256) k_density_exact(float4* __restrict__ spos
         }
     });
     if (RECORD) xc[particle] = (uint32_t)count;
-    // The reference writes .w in place while other work-items read .xyz only; here every
-    // thread has read all it needs before any write lands on a different particle, because
-    // the writes only touch .w which no thread of this kernel reads.
+    // The reference writes .w in place while other work-items read .xyz only. Here the
+    // candidates' positions are loaded as whole float4s, so a load may race with another
+    // thread's write of that particle's .w; the loaded .w is never used (the sums take .xyz
+    // only), so the race cannot change a result.
     if (count > 2) {
         density = fmaxf(1.0f, __fmul_rn(__fmul_rn(kp.mass, kp.kconst), density));
         reinterpret_cast<float*>(spos)[4 * (size_t)particle + 3] = density;
@@ -755,20 +768,19 @@ __device__ __forceinline__ void lane_map_init(LaneMap& L) {
 // sub-list of nbr[gi][NBR_CAP] (in candidate order); the lists' lengths are the counts the
 // reference's count > 2 test uses and go to nbr_meta[gi] (one byte per sub-list), or
 // nbr_meta[gi] = NBR_SCAN when a sub-list overflowed or the brick could not be staged.
+typedef uint8_t SubListCounts[BRICK_WARPS][GROUP_MAX][NBR_SUBLISTS];  // sub-list lengths per warp group
+
+// The body of k_density_brick, on shared memory the caller provides: s_buf (DENSITY_SMEM
+// bytes), S, L and wcnt. The batched step's persistent kernel runs it as one of its phases.
+// Returns false if a bulk-copy wait gave up (the CTA left the loop).
 template <int DIMS, bool BATCH>
-__global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __restrict__ spos,
-                                                                 float4* __restrict__ svel,
-                                                                 const uint2* __restrict__ table,
-                                                                 const uint32_t* __restrict__ bricks,
-                                                                 uint32_t* counters, KParams kp,
-                                                                 uint16_t* __restrict__ nbr,
-                                                                 uint64_t* __restrict__ nbr_meta, uint32_t* err) {
+__device__ __forceinline__ bool density_brick_run(float4* s_buf, BrickShared& S, LaneMap& L, SubListCounts& wcnt,
+                                                  float4* __restrict__ spos, float4* __restrict__ svel,
+                                                  const uint2* __restrict__ table, const uint32_t* __restrict__ bricks,
+                                                  uint32_t* counters, const KParams& kp, uint16_t* __restrict__ nbr,
+                                                  uint64_t* __restrict__ nbr_meta, uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;  // the brick's own row
-    extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, then per-warp neighbour lists
-    __shared__ BrickShared S;
-    __shared__ LaneMap L;
-    __shared__ __align__(8) uint8_t wcnt[BRICK_WARPS][GROUP_MAX][NBR_SUBLISTS];  // sub-list lengths
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * GROUP_MAX * WLIST_STRIDE;
     lane_map_init(L);
@@ -777,7 +789,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
         fence_mbar_init();
     }
     uint32_t phase = 0;
-    const uint32_t n_bricks = counters[0];
+    const uint32_t n_bricks = __ldcg(counters);  // written by the bounds pass (an earlier kernel or phase)
     const float h2 = kp.h2, thr = kp.r2_thresh;
     const uint32_t buf_a = smem_addr(s_buf);
     // the next brick's id is fetched while this one is processed
@@ -791,7 +803,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
         int x0, ncell;
         brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         const bool staged = brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr);
-        if (staged && !brick_wait(S, phase, err)) return;
+        if (staged && !brick_wait(S, phase, err)) return false;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
             for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
@@ -925,6 +937,22 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
         }
         if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
+    return true;
+}
+
+template <int DIMS, bool BATCH>
+__global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __restrict__ spos,
+                                                                 float4* __restrict__ svel,
+                                                                 const uint2* __restrict__ table,
+                                                                 const uint32_t* __restrict__ bricks,
+                                                                 uint32_t* counters, KParams kp,
+                                                                 uint16_t* __restrict__ nbr,
+                                                                 uint64_t* __restrict__ nbr_meta, uint32_t* err) {
+    extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, then per-warp neighbour lists
+    __shared__ BrickShared S;
+    __shared__ LaneMap L;
+    __shared__ __align__(8) SubListCounts wcnt;
+    density_brick_run<DIMS, BATCH>(s_buf, S, L, wcnt, spos, svel, table, bricks, counters, kp, nbr, nbr_meta, err);
 }
 
 // Pressure + viscosity contribution of one in-range neighbour (acc: pressure xyz, viscosity xyz).
@@ -986,26 +1014,22 @@ __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& v
 // scan the rows in global memory. With FUSED the clip-box, integrate-force, gravity and
 // integrate-velocity stages follow in registers; otherwise the SPH force is added to
 // force[index[i]] (with w = 0) as clCalculateForces does.
-template <int DIMS, bool FUSED, bool BATCH>
-__global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* __restrict__ spos,
-                                                               const float4* __restrict__ svel,
-                                                               const uint32_t* __restrict__ index,
-                                                               float4* __restrict__ pos,
-                                                               float4* __restrict__ vel,
-                                                               float4* __restrict__ force,
-                                                               const uint2* __restrict__ table,
-                                                               const uint32_t* __restrict__ bricks,
-                                                               uint32_t* counters, KParams kp,
-                                                               const uint16_t* __restrict__ nbr,
-                                                               const uint64_t* __restrict__ nbr_meta,
-                                                               uint32_t* err) {
+// The body of k_force_brick, on shared memory the caller provides: s_buf (FORCE_SMEM bytes:
+// [BRICK_CAP] positions, [BRICK_CAP] velocities, then the neighbour lists of up to
+// LIST_STAGE_MAX targets), S and L. COH: the sorted state and the lists were written earlier
+// in the same launch, so the direct loads of them go through L2 only. Returns false if a
+// bulk-copy wait gave up (the CTA left the loop).
+template <int DIMS, bool FUSED, bool BATCH, bool COH = false>
+__device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, LaneMap& L,
+                                                const float4* __restrict__ spos, const float4* __restrict__ svel,
+                                                const uint32_t* __restrict__ index, float4* __restrict__ pos,
+                                                float4* __restrict__ vel, float4* __restrict__ force,
+                                                const uint2* __restrict__ table, const uint32_t* __restrict__ bricks,
+                                                uint32_t* counters, const KParams& kp,
+                                                const uint16_t* __restrict__ nbr,
+                                                const uint64_t* __restrict__ nbr_meta, uint32_t* err) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     constexpr int RC = DIMS == 3 ? 4 : 1;
-    // [BRICK_CAP] positions, [BRICK_CAP] velocities, then the neighbour lists of up to
-    // LIST_STAGE_MAX targets
-    extern __shared__ float4 s_buf[];
-    __shared__ BrickShared S;
-    __shared__ LaneMap L;
     const int t = threadIdx.x, lane = t & 31;
     lane_map_init(L);
     if (t == 0) {
@@ -1013,7 +1037,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
         fence_mbar_init();
     }
     uint32_t phase = 0;
-    const uint32_t n_bricks = counters[0];
+    const uint32_t n_bricks = __ldcg(counters);  // written by the bounds pass (an earlier kernel or phase)
     const float4* s_pos = s_buf;
     const float4* s_vel = s_buf + BRICK_CAP;
     uint16_t* s_lists = reinterpret_cast<uint16_t*>(s_buf + 2 * BRICK_CAP);
@@ -1062,7 +1086,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
         __syncthreads();
         const bool staged = S.total <= BRICK_CAP && S.total > 0;
         if (staged) {
-            if (!brick_wait(S, phase, err)) return;
+            if (!brick_wait(S, phase, err)) return false;
             // w lanes of the staged copies: 1/rho and p/rho (force_pair_pre)
             for (uint32_t k = t; k < S.total; k += BRICK_THREADS) {
                 const float a = rcp_approx(s_buf[k].w);
@@ -1095,17 +1119,17 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                 const uint32_t f = L.info[min(GROUP_MAX, nt - g0)];
                 Q = f & 0xFFu;
                 sub = f >> 8;
-                pi = staged ? s_pos[S.base[RC] + tl] : spos[gi];
-                vi = staged ? s_vel[S.base[RC] + tl] : svel[gi];
+                pi = staged ? s_pos[S.base[RC] + tl] : ld_phase<COH>(spos + gi);
+                vi = staged ? s_vel[S.base[RC] + tl] : ld_phase<COH>(svel + gi);
                 if (p == 0) {  // prefetch what the integration needs
-                    o = (staged && lists_staged) ? s_index[gi - (tfirst & ~3u)] : index[gi];
+                    o = (staged && lists_staged) ? s_index[gi - (tfirst & ~3u)] : ld_phase<COH>(index + gi);
                     f_o = force[o];
                     if (FUSED) {
                         v_o = vel[o];
                         p_o = pos[o];
                     }
                 }
-                meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : nbr_meta[gi]);
+                meta = !staged ? NBR_SCAN : (lists_staged ? s_meta[gi - (tfirst & ~1u)] : ld_phase<COH>(nbr_meta + gi));
             }
             const bool scan = (meta & NBR_SCAN) != 0;
             // Sub-lists that start on 16-byte chunks and pair up (Q = 2, 4, 8) can be walked a
@@ -1147,7 +1171,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
 #pragma unroll 1
                         for (uint32_t i = 0; i < m; ++i) {
                             const uint32_t s = q * sub + k;
-                            const uint32_t i0 = lst[(s >> 3) * n8 + (s & 7u)];
+                            const uint32_t i0 = ld_phase<COH>(lst + (s >> 3) * n8 + (s & 7u));
                             force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
                             k += dk;
                             settle();
@@ -1158,7 +1182,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                             const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u;
                             const uint4* l4 = reinterpret_cast<const uint4*>(lst);
                             for (uint32_t k0 = 0; k0 < n; k0 += 8) {
-                                const uint4 v = l4[(size_t)((q * sub + k0) >> 3) * ntarg];
+                                const uint4 v = ld_phase<COH>(l4 + (size_t)((q * sub + k0) >> 3) * ntarg);
                                 const uint32_t w[4] = {v.x, v.y, v.z, v.w};
                                 const uint32_t m = min(8u, n - k0);
 #pragma unroll
@@ -1177,14 +1201,15 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                         const float4* rv = svel + S.lo[r];
                         const uint32_t hi = S.off[r][c + 3];
                         for (uint32_t j = S.off[r][c] + p; j < hi; j += P) {
-                            const float4 pj = rp[j];
+                            const float4 pj = ld_phase<COH>(rp + j);
                             const float dx = pi.x - pj.x, dy = pi.y - pj.y;
                             float r2 = fmaf(dy, dy, dx * dx);
                             if (DIMS == 3) {
                                 const float dz = pi.z - pj.z;
                                 r2 = fmaf(dz, dz, r2);
                             }
-                            if (r2 < kp.r2_thresh && r2 > 0.0f) force_pair<DIMS>(pi, vi, inv_rho_i, pj, rv[j], kp.h, acc);
+                            if (r2 < kp.r2_thresh && r2 > 0.0f)
+                                force_pair<DIMS>(pi, vi, inv_rho_i, pj, ld_phase<COH>(rv + j), kp.h, acc);
                         }
                     }
                 }
@@ -1254,6 +1279,27 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
         }
         if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
+    return true;
+}
+
+template <int DIMS, bool FUSED, bool BATCH>
+__global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* __restrict__ spos,
+                                                               const float4* __restrict__ svel,
+                                                               const uint32_t* __restrict__ index,
+                                                               float4* __restrict__ pos,
+                                                               float4* __restrict__ vel,
+                                                               float4* __restrict__ force,
+                                                               const uint2* __restrict__ table,
+                                                               const uint32_t* __restrict__ bricks,
+                                                               uint32_t* counters, KParams kp,
+                                                               const uint16_t* __restrict__ nbr,
+                                                               const uint64_t* __restrict__ nbr_meta,
+                                                               uint32_t* err) {
+    extern __shared__ float4 s_buf[];
+    __shared__ BrickShared S;
+    __shared__ LaneMap L;
+    force_brick_run<DIMS, FUSED, BATCH>(s_buf, S, L, spos, svel, index, pos, vel, force, table, bricks, counters, kp,
+                                        nbr, nbr_meta, err);
 }
 
 }  // namespace gbsph

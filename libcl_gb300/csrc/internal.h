@@ -16,7 +16,8 @@ enum : uint32_t {
     DEV_ERR_LOOKBACK_TIMEOUT = 1u,  // decoupled look-back spin hit its limit
     DEV_ERR_MBAR_TIMEOUT = 2u,      // bulk-copy mbarrier wait hit its limit
     DEV_ERR_KEY_RANGE = 4u,         // a key fell outside its cell table
-    DEV_ERR_CAPACITY = 8u           // a fixed-capacity list overflowed
+    DEV_ERR_CAPACITY = 8u,          // a fixed-capacity list overflowed
+    DEV_ERR_GRID_TIMEOUT = 16u      // a persistent kernel's grid-wide barrier wait hit its limit
 };
 
 int dev_err_to_status(uint32_t bits);
@@ -56,8 +57,9 @@ constexpr size_t SORT_HEADER_BYTES = 4352;
 constexpr size_t SORT_USER_COUNTER_OFFSET = 4112;  // 60 uint32 free for callers
 constexpr uint32_t SORT_MAX_KEYS = (1u << 30) - 1u;
 
-__host__ __device__ inline int sort_passes(int start_bit, int end_bit) {
-    return (end_bit - start_bit + SORT_RADIX_BITS - 1) / SORT_RADIX_BITS;
+// Passes of a sort on bits [start_bit, end_bit) with `digit`-bit digits (1 to 8).
+__host__ __device__ inline int sort_passes(int start_bit, int end_bit, int digit = SORT_RADIX_BITS) {
+    return (end_bit - start_bit + digit - 1) / digit;
 }
 __host__ __device__ inline uint32_t sort_tiles(uint32_t n, uint32_t tile = SORT_MIN_TILE) { return (n + tile - 1) / tile; }
 // Keys per thread of a pass over n keys: small sorts use small tiles (more tiles in flight,
@@ -85,6 +87,8 @@ struct OnesweepArgs {
     uint32_t* err = nullptr;
     SortGather gather;
     cudaEvent_t before_last = nullptr;  // if set: the last pass waits for it (its gather's inputs)
+    int digit_bits = SORT_RADIX_BITS;   // bits per pass (1 to 8, at most SORT_MAX_PASSES passes)
+    int items = 0;                      // keys per thread of a tile (8 or 16); 0: by key count
 };
 
 // Zeroes the scratch header and the look-back words.

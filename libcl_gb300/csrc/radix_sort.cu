@@ -21,44 +21,12 @@
 #include <string>
 
 #include "device.cuh"
+#include "grid_sync.cuh"
 #include "internal.h"
+#include "onesweep.cuh"
 
 namespace gbsph {
 namespace {
-
-constexpr uint32_t FLAG_AGG = 1u << 30;
-constexpr uint32_t FLAG_PREFIX = 2u << 30;
-constexpr uint32_t COUNT_MASK = (1u << 30) - 1u;
-constexpr int SORT_WARPS = SORT_THREADS / 32;
-
-static_assert(SORT_THREADS == SORT_RADIX, "one thread per digit in the per-digit phases");
-
-// Exclusive scan of one value per thread over a 256-thread block. `s_tmp` holds 8 words.
-__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_tmp) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_tmp[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < SORT_WARPS ? s_tmp[lane] : 0u;
-        uint32_t incl = w;
-#pragma unroll
-        for (int o = 1; o < SORT_WARPS; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane < SORT_WARPS) s_tmp[lane] = incl - w;
-    }
-    __syncthreads();
-    uint32_t r = x - v + s_tmp[warp];
-    __syncthreads();  // s_tmp may be reused by the caller
-    return r;
-}
 
 __global__ void __launch_bounds__(512) k_sort_hist(const uint32_t* __restrict__ keys, uint32_t n,
                                                    int start_bit, int end_bit,
@@ -90,137 +58,12 @@ __global__ void __launch_bounds__(SORT_THREADS, onesweep_min_blocks(ITEMS)) k_on
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint32_t n, int shift,
     int bits, int pass, uint32_t tiles, uint32_t* __restrict__ scratch, uint32_t* err,
     SortGather gather) {
-    static_assert(ITEMS % 2 == 0, "ranks are packed two per register");
-    constexpr int TILE = SORT_THREADS * ITEMS;
-    __shared__ uint32_t s_keys[TILE];
-    __shared__ uint32_t s_vals[TILE];
-    __shared__ uint32_t s_whist[SORT_WARPS * SORT_RADIX];
-    __shared__ uint32_t s_base[SORT_RADIX];
-    __shared__ uint32_t s_tmp[SORT_WARPS];
-    __shared__ uint32_t s_tile;
-
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t* hist = scratch + pass * SORT_RADIX;
-    uint32_t* counter = scratch + 4096 / 4 + pass;
-    uint32_t* status = scratch + SORT_HEADER_BYTES / 4 + (size_t)pass * tiles * SORT_RADIX;
-
-    if (t == 0) s_tile = atomicAdd(counter, 1u);
-    for (int i = t; i < SORT_WARPS * SORT_RADIX; i += SORT_THREADS) s_whist[i] = 0;
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    if (tile >= tiles) {  // counter not reset since the last sort: refuse rather than overrun
-        if (t == 0) atomicOr(err, DEV_ERR_CAPACITY);
-        return;
-    }
-    const uint32_t base = tile * TILE;
-    const uint32_t mask = (1u << bits) - 1u;
-
-    // Load: warp-striped, so item order inside the tile is (warp, i, lane) == index order.
-    // The keys wait in the value half of the tile buffer (each warp its own slice) until the
-    // scatter, which keeps the register count low enough for five CTAs per SM.
-    uint32_t* stash = s_vals + warp * 32 * ITEMS + lane;
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t idx = base + (uint32_t)(warp * 32 * ITEMS + i * 32 + lane);
-        stash[i * 32] = idx < n ? keys_in[idx] : 0xFFFFFFFFu;  // padding sorts last in the top digit
-    }
-    __syncwarp();
-
-    // Rank within the warp: peers of equal digit = AND over the digit's bits of the ballot or
-    // its complement (digits narrower than 8 bits have zero high bits, whose ballots are
-    // empty and leave the mask alone). All peers read the warp's digit counter, then the
-    // lowest peer advances it. Ranks are < 2^16 and stored two per register.
-    uint32_t* wh = s_whist + warp * SORT_RADIX;
-    const uint32_t lt = lanemask_lt();
-    uint32_t r[ITEMS / 2];
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t d = (stash[i * 32] >> shift) & mask;
-        uint32_t peers = 0xffffffffu;
-#pragma unroll
-        for (int b = 0; b < SORT_RADIX_BITS; ++b) {
-            const uint32_t bit = (d >> b) & 1u;
-            peers &= __ballot_sync(0xffffffffu, bit) ^ (bit - 1u);
-        }
-        const uint32_t old = wh[d];
-        __syncwarp();
-        if ((uint32_t)lane == __ffs(peers) - 1u) wh[d] = old + __popc(peers);
-        const uint32_t rank = old + __popc(peers & lt);
-        r[i >> 1] = (i & 1) ? (r[i >> 1] | rank << 16) : rank;
-        __syncwarp();
-    }
-    __syncthreads();
-
-    // Thread t owns digit t: tile count, then each warp's start of digit t inside the tile
-    // (tile-local start + the counts of the warps before it).
-    uint32_t cnt = 0;
-#pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) {
-        const uint32_t c = s_whist[w * SORT_RADIX + t];
-        s_whist[w * SORT_RADIX + t] = cnt;
-        cnt += c;
-    }
-    const uint32_t tstart = block_exclusive_scan(cnt, s_tmp);
-#pragma unroll
-    for (int w = 0; w < SORT_WARPS; ++w) s_whist[w * SORT_RADIX + t] += tstart;
-    const uint32_t goff = block_exclusive_scan(hist[t], s_tmp);
-
-    // Decoupled look-back for digit t.
-    uint32_t excl = 0;
-    if (tile == 0) {
-        st_relaxed_gpu(&status[t], FLAG_PREFIX | cnt);
-    } else {
-        st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_AGG | cnt);
-        int pred = (int)tile - 1;
-        WaitBudget budget;
-        while (pred >= 0) {
-            const uint32_t s = ld_relaxed_gpu(&status[(size_t)pred * SORT_RADIX + t]);
-            if ((s & ~COUNT_MASK) == 0u) {
-                if (budget.expired()) {
-                    atomicOr(err, DEV_ERR_LOOKBACK_TIMEOUT);
-                    break;
-                }
-                continue;
-            }
-            excl += s & COUNT_MASK;
-            if (s & FLAG_PREFIX) break;
-            --pred;
-        }
-        st_relaxed_gpu(&status[(size_t)tile * SORT_RADIX + t], FLAG_PREFIX | ((excl + cnt) & COUNT_MASK));
-    }
-    s_base[t] = goff + excl - tstart;
-    uint32_t k[ITEMS];
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) k[i] = stash[i * 32];
-    __syncthreads();
-
-    // Tile-local sorted order in shared memory; values are read here, after the ranking.
-#pragma unroll
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t idx = base + (uint32_t)(warp * 32 * ITEMS + i * 32 + lane);
-        const uint32_t pos = s_whist[warp * SORT_RADIX + ((k[i] >> shift) & mask)] + ((r[i >> 1] >> (16 * (i & 1))) & 0xffffu);
-        s_keys[pos] = k[i];
-        s_vals[pos] = IOTA ? idx : (idx < n ? vals_in[idx] : 0u);
-    }
-    __syncthreads();
-
-    // Each digit's run goes to one contiguous range of the output.
-    const uint32_t valid = min((uint32_t)TILE, n - base);
-#pragma unroll 4
-    for (int i = 0; i < ITEMS; ++i) {
-        const uint32_t j = (uint32_t)(i * SORT_THREADS + t);
-        if (j < valid) {
-            const uint32_t key = s_keys[j], val = s_vals[j];
-            const uint32_t dst = s_base[(key >> shift) & mask] + j;
-            if (dst >= n) {  // histogram inconsistent with the keys (misuse): never write out of range
-                atomicOr(err, DEV_ERR_KEY_RANGE);
-                continue;
-            }
-            keys_out[dst] = key;
-            vals_out[dst] = val;
-            if (NGATHER > 0) gather.dst[0][dst] = __ldg(gather.src[0] + val);
-            if (NGATHER > 1) gather.dst[1][dst] = __ldg(gather.src[1] + val);
-        }
+    __shared__ __align__(16) uint32_t s_w[onesweep_smem_words(ITEMS)];
+    const OnesweepSmem sm = onesweep_smem<ITEMS>(s_w);
+    if (!onesweep_tile<IOTA, NGATHER, ITEMS>(sm, keys_in, vals_in, keys_out, vals_out, n, shift, bits, pass, tiles,
+                                             scratch, err, gather)) {
+        // counter not reset since the last sort: refuse rather than overrun
+        if (threadIdx.x == 0) atomicOr(err, DEV_ERR_CAPACITY);
     }
 }
 
@@ -263,8 +106,8 @@ cudaError_t launch_pass_items(int ngather, const uint32_t* kin, const uint32_t* 
 template <bool IOTA>
 cudaError_t launch_pass(int ngather, const uint32_t* kin, const uint32_t* vin, uint32_t* kout,
                         uint32_t* vout, uint32_t n, int shift, int bits, int pass, uint32_t* scratch,
-                        uint32_t* err, const SortGather& g, cudaStream_t s) {
-    if (sort_items_for(n) == 8)
+                        uint32_t* err, const SortGather& g, cudaStream_t s, int items) {
+    if (items == 8)
         return launch_pass_items<IOTA, 8>(ngather, kin, vin, kout, vout, n, shift, bits, pass, scratch, err, g, s);
     return launch_pass_items<IOTA, 16>(ngather, kin, vin, kout, vout, n, shift, bits, pass, scratch, err, g, s);
 }
@@ -284,7 +127,39 @@ __global__ void k_selftest_mbar(uint32_t* err) {
     }
 }
 
+// Two CTAs at a grid barrier that waits for three: the bounded wait gives up, sets
+// DEV_ERR_GRID_TIMEOUT and the abort flag, and both CTAs leave (failure-detection self-test
+// of the persistent batch step's barrier).
+__global__ void k_selftest_grid(uint32_t* words, uint32_t* err) {
+    __shared__ uint32_t s_flag;
+    GridSync gs{words, err, 0u, gridDim.x + 1u};
+    gs.sync(&s_flag);
+}
+
 }  // namespace
+
+int selftest_grid_timeout(cudaStream_t s) {
+    uint32_t* words = nullptr;
+    if (cudaMalloc(&words, 256) != cudaSuccess) {
+        cudaGetLastError();
+        return GBSPH_ERR_OUT_OF_MEMORY;
+    }
+    int rc = GBSPH_OK;
+    uint32_t bits = 0;
+    uint32_t* err = words + 32;
+    if (cudaMemsetAsync(words, 0, 256, s) != cudaSuccess) {
+        rc = GBSPH_ERR_CUDA;
+    } else {
+        k_selftest_grid<<<2, 64, 0, s>>>(words, err);
+        if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess ||
+            cudaMemcpy(&bits, err, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = GBSPH_ERR_CUDA;
+        else
+            rc = (bits & DEV_ERR_GRID_TIMEOUT) ? GBSPH_ERR_DEVICE_TIMEOUT : GBSPH_OK;
+    }
+    cudaFree(words);
+    return rc;
+}
 
 int selftest_mbarrier_timeout(cudaStream_t s) {
     uint32_t* err = nullptr;
@@ -334,24 +209,29 @@ cudaError_t onesweep_histogram(const uint32_t* keys, uint32_t n, int start_bit, 
 }
 
 cudaError_t onesweep_passes(const OnesweepArgs& a, cudaStream_t s) {
-    const int P = sort_passes(a.start_bit, a.end_bit);
+    const int digit = a.digit_bits;
+    if (digit < 1 || digit > SORT_RADIX_BITS) return cudaErrorInvalidValue;
+    const int P = sort_passes(a.start_bit, a.end_bit, digit);
     if (a.n == 0 || P == 0) return cudaSuccess;
+    if (P > SORT_MAX_PASSES) return cudaErrorInvalidValue;
+    const int items = a.items ? a.items : sort_items_for(a.n);
+    if (items != 8 && items != 16) return cudaErrorInvalidValue;
     const uint32_t* kin = a.keys_in;
     const uint32_t* vin = a.vals_in;
     for (int p = 0; p < P; ++p) {
         const bool last = p == P - 1;
         uint32_t* kout = last ? a.keys_out : a.tmp_keys[p & 1];
         uint32_t* vout = last ? a.vals_out : a.tmp_vals[p & 1];
-        const int shift = a.start_bit + p * SORT_RADIX_BITS;
-        const int bits = std::min(SORT_RADIX_BITS, a.end_bit - shift);
+        const int shift = a.start_bit + p * digit;
+        const int bits = std::min(digit, a.end_bit - shift);
         const int ng = last ? a.gather.n_gather : 0;
         if (last && a.before_last) {
             cudaError_t e = cudaStreamWaitEvent(s, a.before_last, 0);
             if (e != cudaSuccess) return e;
         }
         cudaError_t e = (vin == nullptr)
-            ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s)
-            : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s);
+            ? launch_pass<true>(ng, kin, nullptr, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s, items)
+            : launch_pass<false>(ng, kin, vin, kout, vout, a.n, shift, bits, p, (uint32_t*)a.scratch, a.err, a.gather, s, items);
         if (e != cudaSuccess) return e;
         kin = kout;
         vin = vout;
@@ -525,9 +405,10 @@ GBSPH_API int gbsph_radix_sort_sync_status(gbsph_radix_sort_t h, void* stream) {
 int selftest_noalloc_timeout(cudaStream_t s);  // below, beside the static scratch array
 
 GBSPH_API int gbsph_selftest_bounded_wait(int which, void* stream) {
-    if (which < 0 || which > 2) return GBSPH_ERR_ARGUMENT;
+    if (which < 0 || which > 3) return GBSPH_ERR_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
     if (which == 1) return selftest_mbarrier_timeout(s);
+    if (which == 3) return selftest_grid_timeout(s);
     if (which == 2) return selftest_noalloc_timeout(s);
     // Two tiles of 2048 keys; the pass's tile counter starts at 1, so tile 0 never runs, the
     // CTA that draws tile 1 looks back at tile 0's unwritten status until its bound expires,

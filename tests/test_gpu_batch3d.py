@@ -5,7 +5,9 @@ import numpy as np
 import pytest
 
 from fluid_helpers import make_fluid, state
-from libcl_gb300 import (BUF_FORCE, BUF_INDEX, BUF_POSITION, BUF_VELOCITY, OPT_BRICK_WIDTH, Batch3D)
+from libcl_gb300 import (BUF_CELL, BUF_FORCE, BUF_INDEX, BUF_POSITION, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY,
+                         BUF_VELOCITY, OPT_BRICK_WIDTH, OPT_PERSISTENT, OPT_RADIX_BITS, OPT_SORT_TILE, Batch3D,
+                         GbsphError)
 from libcl_gb300.scenes import batched_ensemble
 
 pytestmark = pytest.mark.gpu
@@ -79,14 +81,103 @@ def test_autotune_restores_state(cuda):
     import torch
     b = batched_ensemble(n_scenes=16, seed=3, n_min=2000, n_max=40000)
     bt = load_batch(b)
-    before = bt.buffer(BUF_POSITION).cpu().numpy().copy()
+    before = {w: bt.buffer(w).cpu().numpy().copy() for w in (BUF_POSITION, BUF_VELOCITY, BUF_FORCE)}
     best = bt.autotune()
     assert best in (4, 8, 16)
-    after = bt.buffer(BUF_POSITION).cpu().numpy()
-    assert np.array_equal(before, after)
+    cfg = bt.config()
+    assert cfg["brick_width"] == best and cfg["radix_bits"] in (6, 7, 8) and cfg["sort_tile_items"] in (8, 16)
+    assert cfg["persistent"] in (0, 1)
+    for w, v in before.items():
+        assert np.array_equal(v, bt.buffer(w).cpu().numpy()), w
     bt.compute()
     torch.cuda.synchronize()
     assert bt.sync_status() == 0
+
+
+ALL_BUFFERS = (BUF_POSITION, BUF_VELOCITY, BUF_FORCE, BUF_INDEX, BUF_CELL, BUF_SORTED_POSITION, BUF_SORTED_VELOCITY)
+
+
+def _run_batch(b, steps, persistent=0, items=0, bits=8, bw=8):
+    import torch
+    bt = load_batch(b, bw=bw)
+    bt.set_option(OPT_PERSISTENT, persistent)
+    bt.set_option(OPT_SORT_TILE, items)
+    bt.set_option(OPT_RADIX_BITS, bits)
+    for _ in range(steps):
+        bt.compute()
+    torch.cuda.synchronize()
+    assert bt.sync_status() == 0
+    return {w: bt.buffer(w).cpu().numpy().view(np.uint32).copy() for w in ALL_BUFFERS}
+
+
+@pytest.mark.parametrize("bits,items", [(6, 8), (7, 16), (8, 8), (5, 16)])
+def test_sort_digit_width_and_tile_do_not_change_results(cuda, bits, items):
+    """The radix sort is stable, so every digit width and tile size yields the same sorted
+    order and the same step, bit for bit (3 steps of a 12-scene batch whose keys need 17
+    bits: four passes with 5-bit digits, three with 6, 7 or 8)."""
+    b = batched_ensemble(n_scenes=12, seed=21, n_min=1000, n_max=60000)
+    rng = np.random.default_rng(2)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    ref = _run_batch(b, 3)
+    got = _run_batch(b, 3, items=items, bits=bits)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+@pytest.mark.parametrize("items,bits,bw", [(8, 8, 8), (16, 7, 4), (16, 8, 16), (8, 6, 8)])
+def test_persistent_step_matches_staged(cuda, items, bits, bw):
+    """The persistent form (one cooperative kernel per step) and the staged graph run the same
+    phases in the same order, so 4 steps of a 9-scene batch agree bit for bit in every buffer:
+    state, sorted state (density and pressure in .w), sort permutation and cell keys."""
+    b = batched_ensemble(n_scenes=9, seed=31, n_min=800, n_max=50000)
+    rng = np.random.default_rng(8)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    ref = _run_batch(b, 4, 0, items, bits, bw)
+    got = _run_batch(b, 4, 1, items, bits, bw)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+def test_persistent_step_dense_clumps_match_staged(cuda):
+    """Dense, disordered scenes (particles jittered by up to 0.9 spacing, cells of 1 to 20
+    particles): bricks too full to stage and targets whose lists overflow take the direct
+    global-memory paths of the density and force phases."""
+    b = batched_ensemble(n_scenes=5, seed=13, n_min=3000, n_max=40000)
+    rng = np.random.default_rng(4)
+    b.pos[:, :3] += (0.006 + rng.uniform(-0.009, 0.009, (b.n, 3))).astype(np.float32)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    ref = _run_batch(b, 3, 0, bw=16)
+    got = _run_batch(b, 3, 1, bw=16)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+def test_persistent_full_ensemble_matches_staged(cuda):
+    """The 256-scene ensemble (17.3M particles), two steps in each form, bitwise."""
+    import torch
+    b = batched_ensemble()
+    rng = np.random.default_rng(6)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    ref = _run_batch(b, 2, 0, bw=8)
+    torch.cuda.empty_cache()
+    got = _run_batch(b, 2, 1, bw=8)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+def test_batch_options(cuda):
+    b = batched_ensemble(n_scenes=3, seed=1, n_min=1000, n_max=2000)
+    bt = load_batch(b)
+    assert bt.config() == {"brick_width": 8, "radix_bits": 8, "sort_tile_items": 0, "cuda_graph": 1,
+                           "persistent": 0}
+    for opt, bad in ((OPT_RADIX_BITS, 4), (OPT_RADIX_BITS, 9), (OPT_SORT_TILE, 12), (OPT_BRICK_WIDTH, 0)):
+        with pytest.raises(GbsphError):
+            bt.set_option(opt, bad)
+    bt.set_option(OPT_RADIX_BITS, 7)
+    bt.set_option(OPT_SORT_TILE, 16)
+    bt.set_option(OPT_PERSISTENT, 1)
+    assert bt.get_option(OPT_RADIX_BITS) == 7 and bt.get_option(OPT_SORT_TILE) == 16
+    assert bt.get_option(OPT_PERSISTENT) == 1
 
 
 def test_full_ensemble_against_oracle_and_scenes_run_alone(cuda):

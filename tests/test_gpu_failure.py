@@ -3,8 +3,10 @@ GBSPH_ERR_DEVICE_TIMEOUT through the host, and leave the context usable.
 
 gbsph_selftest_bounded_wait(0) runs the one-sweep sort pass with its tile counter started at
 1, so the look-back of tile 1 waits on tile 0's status, which nothing writes;
-gbsph_selftest_bounded_wait(1) waits on an mbarrier expecting bytes that no copy delivers.
-Both waits are bounded by about one second of device time."""
+gbsph_selftest_bounded_wait(1) waits on an mbarrier expecting bytes that no copy delivers;
+gbsph_selftest_bounded_wait(3) has two CTAs wait at the persistent batch step's grid-wide
+barrier for a third that does not exist. Each wait is bounded by about one second of device
+time."""
 import time
 
 import numpy as np
@@ -15,7 +17,7 @@ from libcl_gb300 import ERR_ARGUMENT, ERR_DEVICE_TIMEOUT, OK, RadixSort, load_li
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("which", [0, 1])
+@pytest.mark.parametrize("which", [0, 1, 3])
 def test_bounded_wait_times_out_and_context_survives(cuda, which):
     import torch
     lib = load_library()
