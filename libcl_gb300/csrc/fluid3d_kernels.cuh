@@ -1171,7 +1171,9 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
 #pragma unroll 1
                         for (uint32_t i = 0; i < m; ++i) {
                             const uint32_t s = q * sub + k;
-                            const uint32_t i0 = ld_phase<COH>(lst + (s >> 3) * n8 + (s & 7u));
+                            const uint32_t li = (s >> 3) * n8 + (s & 7u);
+                            // staged lists are in shared memory, the others in global memory
+                            const uint32_t i0 = lists_staged ? lst[li] : ld_phase<COH>(lst + li);
                             force_pair_pre<DIMS>(pi, vi, s_pos[i0], s_vel[i0], kp.h, acc);
                             k += dk;
                             settle();
@@ -1182,7 +1184,8 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
                             const uint32_t n = (uint32_t)(meta >> (8 * q)) & 127u;
                             const uint4* l4 = reinterpret_cast<const uint4*>(lst);
                             for (uint32_t k0 = 0; k0 < n; k0 += 8) {
-                                const uint4 v = ld_phase<COH>(l4 + (size_t)((q * sub + k0) >> 3) * ntarg);
+                                const size_t li = (size_t)((q * sub + k0) >> 3) * ntarg;
+                                const uint4 v = lists_staged ? l4[li] : ld_phase<COH>(l4 + li);
                                 const uint32_t w[4] = {v.x, v.y, v.z, v.w};
                                 const uint32_t m = min(8u, n - k0);
 #pragma unroll
