@@ -112,9 +112,10 @@ __device__ __forceinline__ bool onesweep_tile(const OnesweepSmem& sm, const uint
     }
     __syncwarp();
 
-    // Rank within the warp: peers of equal digit = AND over the digit's `bits` bits of the
-    // ballot or its complement. All peers read the warp's digit counter, then the lowest peer
-    // advances it. Ranks are < 2^16 and stored two per register.
+    // Rank within the warp: peers of equal digit = AND over the digit's bits of the ballot or
+    // its complement (digits narrower than 8 bits have zero high bits, whose ballots are
+    // empty and leave the mask alone). All peers read the warp's digit counter, then the
+    // lowest peer advances it. Ranks are < 2^16 and stored two per register.
     uint32_t* wh = s_whist + warp * SORT_RADIX;
     const uint32_t lt = lanemask_lt();
     uint32_t r[ITEMS / 2];
@@ -124,7 +125,6 @@ __device__ __forceinline__ bool onesweep_tile(const OnesweepSmem& sm, const uint
         uint32_t peers = 0xffffffffu;
 #pragma unroll
         for (int b = 0; b < SORT_RADIX_BITS; ++b) {
-            if (b >= bits) break;  // uniform over the block
             const uint32_t bit = (d >> b) & 1u;
             peers &= __ballot_sync(0xffffffffu, bit) ^ (bit - 1u);
         }
