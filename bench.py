@@ -293,11 +293,11 @@ def _time_steps(fn, steps: int, stream) -> float:
     return e0.elapsed_time(e1)
 
 
-def extra_batched(stream, steps: int = 200) -> dict:
+def extra_batched(stream, steps: int = 200, options: dict | None = None, loop: bool = True) -> dict:
     """256 independent scenes (log-uniform 4,096-262,144 particles, 17.3M in all): `steps`
     batched steps in the configuration the autotuner chose (step form, brick width, sort digit
-    width, sort tile), the other step form beside it, and the plain step looped over the same
-    scenes for as many steps."""
+    width, sort tile) or in `options` ({option: value}, no autotuning), the other step form
+    beside it, and (with `loop`) the plain step looped over the same scenes for as many steps."""
     import torch
     from libcl_gb300 import BUF_FORCE, BUF_POSITION, BUF_VELOCITY, OPT_PERSISTENT, Batch3D, Fluid3D
     from libcl_gb300.scenes import batched_ensemble
@@ -307,7 +307,11 @@ def extra_batched(stream, steps: int = 200) -> dict:
     bt.buffer(BUF_POSITION).copy_(torch.from_numpy(b.pos))
     bt.buffer(BUF_VELOCITY).zero_()
     bt.buffer(BUF_FORCE).zero_()
-    bt.autotune(stream)
+    if options is None:
+        bt.autotune(stream)
+    else:
+        for k, v in options.items():
+            bt.set_option(k, v)
     cfg = bt.config()
     for _ in range(3):
         bt.compute(stream)
@@ -320,6 +324,15 @@ def extra_batched(stream, steps: int = 200) -> dict:
     t_o = _time_steps(lambda: bt.compute(stream), steps, stream)
     assert bt.sync_status() == 0
     del bt
+    forms = {cfg["persistent"]: t_b / steps, 1 - cfg["persistent"]: t_o / steps}
+    out = {"scenes": len(b.descs), "particles": b.n, "steps": steps,
+           "config": {"step_form": "persistent" if cfg["persistent"] else "staged graph",
+                      "brick_width": cfg["brick_width"], "radix_bits": cfg["radix_bits"],
+                      "sort_tile_keys": 256 * cfg["sort_tile_items"], "autotuned": options is None},
+           "batched_particle_steps_per_s": b.n * steps / (t_b * 1e-3), "batched_ms_per_step": t_b / steps,
+           "staged_graph_ms_per_step": forms[0], "persistent_ms_per_step": forms[1]}
+    if not loop:
+        return out
     fluids = []
     for s in range(len(b.descs)):
         f = Fluid3D()
@@ -330,16 +343,9 @@ def extra_batched(stream, steps: int = 200) -> dict:
             f.compute(stream)
     t_l = _time_steps(lambda: [f.compute(stream) for f in fluids], steps, stream)
     looped = b.n * steps / (t_l * 1e-3)
-    batched = b.n * steps / (t_b * 1e-3)
-    forms = {cfg["persistent"]: t_b / steps, 1 - cfg["persistent"]: t_o / steps}
-    return {"scenes": len(b.descs), "particles": b.n, "steps": steps,
-            "config": {"step_form": "persistent" if cfg["persistent"] else "staged graph",
-                       "brick_width": cfg["brick_width"], "radix_bits": cfg["radix_bits"],
-                       "sort_tile_keys": 256 * cfg["sort_tile_items"]},
-            "batched_particle_steps_per_s": batched, "looped_particle_steps_per_s": looped,
-            "speedup": batched / looped, "batched_ms_per_step": t_b / steps,
-            "staged_graph_ms_per_step": forms[0], "persistent_ms_per_step": forms[1],
-            "looped_ms_per_step": t_l / steps}
+    out.update({"looped_particle_steps_per_s": looped, "speedup": out["batched_particle_steps_per_s"] / looped,
+                "looped_ms_per_step": t_l / steps})
+    return out
 
 
 def extra_sort(stream) -> dict:
@@ -731,7 +737,20 @@ def main(argv=None) -> int:
                          "262,144-bucket hash with the exact kernels")
     ap.add_argument("--profile-suite", action="store_true",
                     help="run every hot path once, untimed (the workload of the per-kernel ncu summary)")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="run only the 256-scene batched step, both forms, --steps timed steps each, in the "
+                         "configuration given by --brick-width / --radix-bits / --sort-tile (no autotuning, "
+                         "no looped baseline): the workload of the batched step's launch list")
+    ap.add_argument("--radix-bits", type=int, default=8, help="--batched-only: sort digit width")
+    ap.add_argument("--sort-tile", type=int, default=16, help="--batched-only: sort keys per thread (8 or 16)")
     args = ap.parse_args(argv)
+    if args.batched_only:
+        import torch
+        from libcl_gb300 import OPT_BRICK_WIDTH, OPT_RADIX_BITS, OPT_SORT_TILE
+        torch.cuda.set_device(0)
+        opts = {OPT_BRICK_WIDTH: args.brick_width or 16, OPT_RADIX_BITS: args.radix_bits, OPT_SORT_TILE: args.sort_tile}
+        print(json.dumps(extra_batched(torch.cuda.current_stream(), steps=args.steps, options=opts, loop=False)))
+        return 0
     if args.profile_suite:
         import torch
         torch.cuda.set_device(0)

@@ -147,6 +147,7 @@ struct gbsph_batch3d_s {
     int digit_bits = SORT_RADIX_BITS;  // bits per sort pass (5 to 8)
     int sort_items = 0;                // keys per thread of a sort tile (8 or 16; 0: by key count)
     int persistent = 0;                // 1: the step is one cooperative k_batch_step launch
+    bool persistent_graph_ok = true;   // false once capturing the cooperative launch failed
     int step_blocks[2] = {0, 0};       // resident k_batch_step CTAs (8 and 16 keys per thread)
     int dens_blocks = 0, force_blocks = 0;
     cudaStream_t cap_stream = nullptr;
@@ -289,7 +290,8 @@ int enqueue_batch(B* h, const KParams& kp, cudaStream_t s) {
 int sort_items_of(const B* h) { return h->sort_items ? h->sort_items : sort_items_for((uint32_t)h->n); }
 
 // The persistent form: table reset (when needed) and scratch clear, then one cooperative
-// launch. It runs eagerly (three stream operations per step).
+// launch; replayed as a graph like the staged form (eagerly if the driver cannot capture a
+// cooperative launch).
 int enqueue_persistent(B* h, const KParams& kp, cudaStream_t s) {
     const bool clear = h->table_clean;
     if (!clear) GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->cells * sizeof(uint2), s));
@@ -331,13 +333,9 @@ int bcompute(B* h, cudaStream_t s, bool allow_graph) {
         return fail(&h->last_error, GBSPH_ERR_ARGUMENT,
                     std::to_string(kp.digit_bits) + "-bit digits need more than four passes over " +
                         std::to_string(kp.end_bit) + "-bit keys");
-    if (h->persistent) {
-        const int rc = enqueue_persistent(h, kp, s);
-        if (rc) h->table_clean = false;
-        return rc;
-    }
-    if (!h->use_graph || !allow_graph || !h->table_clean) {
-        const int rc = enqueue_batch(h, kp, s);
+    auto enqueue = [&](cudaStream_t st) { return h->persistent ? enqueue_persistent(h, kp, st) : enqueue_batch(h, kp, st); };
+    if (!h->use_graph || !allow_graph || !h->table_clean || (h->persistent && !h->persistent_graph_ok)) {
+        const int rc = enqueue(s);
         if (rc) h->table_clean = false;
         return rc;
     }
@@ -346,20 +344,28 @@ int bcompute(B* h, cudaStream_t s, bool allow_graph) {
     if (!h->gexec || key != h->gkey) {
         binvalidate(h);
         GBSPH_CUDA_TRY(&h->last_error, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_batch(h, kp, h->cap_stream);
+        const int rc = enqueue(h->cap_stream);
         cudaGraph_t g = nullptr;
         const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
-        if (rc || ce != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            h->table_clean = false;
-            return rc ? rc : fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-        }
-        const cudaError_t ie = cudaGraphInstantiate(&h->gexec, g, 0);
-        cudaGraphDestroy(g);
-        if (ie != cudaSuccess) {
+        cudaError_t ie = cudaSuccess;
+        if (!rc && ce == cudaSuccess) ie = cudaGraphInstantiate(&h->gexec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (rc || ce != cudaSuccess || ie != cudaSuccess) {
             h->gexec = nullptr;
             h->table_clean = false;
-            return fail(&h->last_error, GBSPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+            if (h->persistent) {  // a cooperative launch that this driver cannot capture: run it eagerly
+                cudaGetLastError();
+                h->persistent_graph_ok = false;
+                h->last_error = std::string("the persistent step could not be captured (") +
+                                cudaGetErrorString(ce != cudaSuccess ? ce : ie) + "); it runs eagerly";
+                const int rc2 = enqueue(s);
+                if (rc2) h->table_clean = false;
+                return rc2;
+            }
+            if (rc) return rc;
+            return fail(&h->last_error, GBSPH_ERR_CUDA,
+                        std::string(ce != cudaSuccess ? "graph capture: " : "graph instantiate: ") +
+                            cudaGetErrorString(ce != cudaSuccess ? ce : ie));
         }
         h->gkey = key;
     }
