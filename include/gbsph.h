@@ -271,8 +271,10 @@ GBSPH_API int gbsph_fluid3d_compute(gbsph_fluid3d_t h, void* stream);
  * libCL/TEST/main.cpp:222-236): the three float4[n] inputs are uploaded into the fluid's
  * position/velocity/force buffers, the step runs, and the three buffers are downloaded into
  * the outputs (which may be the inputs). With page-locked host memory the uploads of velocity
- * and force overlap the hash, sort and density passes and the whole is one replayed graph;
- * pageable memory works too, without the overlap. Asynchronous on `stream`. */
+ * and force overlap the hash, sort and density passes, the force output (the gravity vector
+ * in every entry when no integrate hook is set) is downloaded while the step computes, and the
+ * whole is one replayed graph; pageable memory works too, without the overlap. The handle
+ * keeps one extra float4[n] device array for the force output. Asynchronous on `stream`. */
 GBSPH_API int gbsph_fluid3d_compute_host(gbsph_fluid3d_t h, const float* position_in, const float* velocity_in,
                                          const float* force_in, float* position_out, float* velocity_out,
                                          float* force_out, void* stream);

@@ -93,7 +93,9 @@ struct gbsph_fluid3d_s {
     std::vector<char> gkey;
     // compute_host: the step with its host copies, captured separately
     cudaStream_t io_stream = nullptr;
-    cudaEvent_t io_ev[3] = {};  // fork, velocity uploaded, force uploaded
+    cudaEvent_t io_ev[5] = {};  // fork, position, velocity and force uploaded, side copies done
+    float4* io_grav = nullptr;  // n copies of the gravity vector: the fused step's force output
+    size_t io_grav_n = 0;
     cudaGraphExec_t gexec_io = nullptr;
     std::vector<char> gkey_io;
     // getParamBuffer: a device copy of `params`, refreshed on the stream before a step whenever
@@ -504,22 +506,34 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
     const bool clear = linear && h->table_clean;
     const size_t bytes = (size_t)kp.n * 16;
     h->ev_valid = false;
+    // Without a hook the fused step leaves the gravity vector in every force entry, so the force
+    // output is known before the step runs: it is downloaded from io_grav on the side stream
+    // while the step computes (after the force input has been read from the same host array).
+    const bool grav_out = io && !h->hook && h->io_grav && h->io_grav_n >= kp.n;
     if (io) {
+        // the uploads one after another on the side stream (position first: the hash needs it;
+        // velocity next: the last sort pass gathers it; force last: the force pass reads it)
         GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[0], s));
         GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(h->io_stream, h->io_ev[0], 0));
-        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 1), io->in[1], bytes, cudaMemcpyHostToDevice, h->io_stream));
-        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[1], h->io_stream));
-        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 2), io->in[2], bytes, cudaMemcpyHostToDevice, h->io_stream));
-        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[2], h->io_stream));
-        GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, 0), io->in[0], bytes, cudaMemcpyHostToDevice, s));
+        for (int w = 0; w < 3; w++) {
+            GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(P4(h, w), io->in[w], bytes, cudaMemcpyHostToDevice, h->io_stream));
+            GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[1 + w], h->io_stream));
+        }
+        if (grav_out) {
+            k_gravity<<<grid1(kp.n), 256, 0, h->io_stream>>>(h->io_grav, kp);
+            GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+            GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(io->out[2], h->io_grav, bytes, cudaMemcpyDeviceToHost, h->io_stream));
+        }
+        GBSPH_CUDA_TRY(&h->last_error, cudaEventRecord(h->io_ev[4], h->io_stream));
     }
     RC(mark(h, 0, s));
     if (linear && !h->table_clean)
         GBSPH_CUDA_TRY(&h->last_error, cudaMemsetAsync(h->table, 0xFF, h->table_cells * sizeof(uint2), s));
     h->table_clean = false;
+    if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[1], 0));
     RC(st_hash(h, kp, s, clear));
     RC(mark(h, 1, s));
-    RC(st_sort(h, kp, s, true, io ? h->io_ev[1] : nullptr));
+    RC(st_sort(h, kp, s, true, io ? h->io_ev[2] : nullptr));
     RC(mark(h, 2, s));
     if (linear) {
         // counters were zeroed with the sort scratch in st_hash
@@ -529,14 +543,14 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
         RC(mark(h, 3, s));
         RC(st_density_brick(h, kp, s));
         RC(mark(h, 4, s));
-        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
+        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[3], 0));
         RC(st_force_brick(h, kp, s, h->hook == nullptr));
     } else {
         RC(st_bounds(h, kp, s, true));
         RC(mark(h, 3, s));
         RC(st_density_exact(h, kp, s, true));
         RC(mark(h, 4, s));
-        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
+        if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[3], 0));
         RC(st_forces_exact(h, kp, s, true));
         if (!h->hook) {
             k_post_fused<<<grid1(kp.n), 256, 0, s>>>(h->spos, h->svel, h->index, P4(h, 0), P4(h, 1), P4(h, 2), kp);
@@ -546,9 +560,11 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
     RC(mark(h, 5, s));
     h->ev_valid = h->opt_profile != 0;
     if (h->hook) RC(run_hook(h, s));
-    if (io)
-        for (int w = 0; w < 3; w++)
+    if (io) {
+        for (int w = 0; w < (grav_out ? 2 : 3); w++)
             GBSPH_CUDA_TRY(&h->last_error, cudaMemcpyAsync(io->out[w], P4(h, w), bytes, cudaMemcpyDeviceToHost, s));
+        GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[4], 0));
+    }
     return GBSPH_OK;
 }
 
@@ -682,6 +698,7 @@ GBSPH_API int gbsph_fluid3d_destroy(gbsph_fluid3d_t h) {
     if (h->dparams) cudaFree(h->dparams);
     if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
     if (h->io_stream) cudaStreamDestroy(h->io_stream);
+    if (h->io_grav) cudaFree(h->io_grav);
     for (auto e : h->io_ev)
         if (e) cudaEventDestroy(e);
     for (auto e : h->ev)
@@ -835,8 +852,9 @@ int compute_impl(H* h, cudaStream_t s, const HostIO* io, bool io_graph) {
     std::vector<char> key = graph_key(h, kp);
     if (io) {
         const size_t o = key.size();
-        key.resize(o + sizeof(HostIO));
+        key.resize(o + sizeof(HostIO) + sizeof(void*));
         std::memcpy(key.data() + o, io, sizeof(HostIO));
+        std::memcpy(key.data() + o + sizeof(HostIO), &h->io_grav, sizeof(void*));
     }
     cudaGraphExec_t& gexec = io ? h->gexec_io : h->gexec;
     std::vector<char>& gkey = io ? h->gkey_io : h->gkey;
@@ -899,6 +917,13 @@ GBSPH_API int gbsph_fluid3d_compute_host(gbsph_fluid3d_t h, const float* positio
     if (!h->io_stream) {
         GBSPH_CUDA_TRY(&h->last_error, cudaStreamCreateWithFlags(&h->io_stream, cudaStreamNonBlocking));
         for (auto& e : h->io_ev) GBSPH_CUDA_TRY(&h->last_error, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    if (h->io_grav_n < h->n) {
+        if (h->io_grav) cudaFree(h->io_grav);
+        h->io_grav = nullptr;
+        h->io_grav_n = 0;
+        GBSPH_CUDA_TRY(&h->last_error, cudaMalloc(&h->io_grav, h->n * sizeof(float4)));
+        h->io_grav_n = h->n;
     }
     const HostIO io{{position_in, velocity_in, force_in}, {position_out, velocity_out, force_out}};
     bool pinned = true;
