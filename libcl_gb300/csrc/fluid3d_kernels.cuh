@@ -542,8 +542,6 @@ static __global__ void k_post_fused(const float4* __restrict__ spos, const float
 // ---- brick (fast, LINEAR_GRID) neighbour kernels ---------------------------------------------
 
 struct BrickShared {
-    uint32_t cnt[9][BRICK_SLOTS];
-    uint32_t st[9][BRICK_SLOTS];
     uint32_t off[9][BRICK_SLOTS + 1];  // lower bounds of each cell inside the row's range
     uint32_t lo[9];                    // first sorted index of the row's range
     uint32_t rcnt[9];
@@ -610,67 +608,69 @@ __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, u
     x0 = bx * W;
     ncell = min(W, nx - x0);
     const uint2* tab = BATCH ? table + S.cell_off : table;
-    for (int idx = t; idx < R * (W + 2); idx += BRICK_THREADS) {
-        const int r = idx / (W + 2), c = idx - r * (W + 2);
+    // a warp per row (warp w takes rows w, w + BRICK_WARPS, ...): lane c reads the range of the
+    // row's column c (cell x0 - 1 + c), a warp scan of the counts gives the columns' offsets
+    // inside the row's range, and the first non-empty column its start
+    const int lane = t & 31;
+    for (int r = t >> 5; r < R; r += BRICK_WARPS) {
         const int cy = y + (r % 3) - 1;
         const int cz = DIMS == 3 ? z + (r / 3) - 1 : 0;
-        const int cx = x0 - 1 + c;
+        const int cx = x0 - 1 + lane;
         uint32_t cnt = 0, st = 0;
-        if (cx >= 0 && cx < nx && cy >= 0 && cy < ny && cz >= 0 && cz < nz) {
+        if (lane < W + 2 && cx >= 0 && cx < nx && cy >= 0 && cy < ny && cz >= 0 && cz < nz) {
             const uint2 e = tab[(uint32_t)cx + (uint32_t)nx * ((uint32_t)cy + (uint32_t)ny * (uint32_t)cz)];
             if (e.x != EMPTY) {
                 cnt = e.y - e.x;
                 st = e.x;
             }
         }
-        S.cnt[r][c] = cnt;
-        S.st[r][c] = st;
-    }
-    __syncthreads();
-    if (t < R) {
-        uint32_t acc = 0, lo = EMPTY;
-        for (int c = 0; c < W + 2; ++c) {
-            S.off[t][c] = acc;
-            if (S.cnt[t][c]) {
-                if (lo == EMPTY) lo = S.st[t][c];
-                acc += S.cnt[t][c];
-            }
+        uint32_t inc = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
         }
-        if (lo == EMPTY) lo = 0;
-        if ((uint64_t)lo + acc > kp.n) {  // inconsistent table: report, use an empty row
-            atomicOr(err, DEV_ERR_KEY_RANGE);
-            for (int c = 0; c < W + 2; ++c) S.off[t][c] = 0;
-            acc = 0;
-            lo = 0;
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        const uint32_t nonempty = __ballot_sync(0xffffffffu, cnt != 0u);
+        const uint32_t lo = nonempty ? __shfl_sync(0xffffffffu, st, __ffs(nonempty) - 1) : 0u;
+        const bool bad = (uint64_t)lo + total > kp.n;  // inconsistent table: report, use an empty row
+        // column W + 2 (and beyond) has no count, so its exclusive offset is the row's total
+        if (lane <= W + 2) S.off[r][lane] = bad ? 0u : inc - cnt;
+        if (lane == 0) {
+            S.lo[r] = bad ? 0u : lo;
+            S.rcnt[r] = bad ? 0u : total;
+            if (bad) atomicOr(err, DEV_ERR_KEY_RANGE);
         }
-        S.off[t][W + 2] = acc;
-        S.lo[t] = lo;
-        S.rcnt[t] = acc;
     }
     __syncthreads();
 }
 
-// Thread 0: compute row bases and issue the copies. Returns (to all threads, after a
-// barrier) whether the brick's rows are staged in shared memory.
+// Warp 0: the rows' bases in the staging buffer (a scan of their counts), then, if the brick
+// fits, lane 0 arms the mbarrier with the byte count and lane r copies row r. Returns (to all
+// threads, after a barrier) whether the brick's rows are staged in shared memory.
 template <int DIMS, int NARR>
 __device__ __forceinline__ bool brick_stage(BrickShared& S, float4* s_buf, uint32_t cap,
                                             const float4* __restrict__ a0, const float4* __restrict__ a1) {
     constexpr int R = DIMS == 3 ? 9 : 3;
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int r = 0; r < R; ++r) {
-            S.base[r] = acc;
-            acc += S.rcnt[r];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const uint32_t rc = lane < R ? S.rcnt[lane] : 0u;
+        uint32_t inc = rc;
+#pragma unroll
+        for (int o = 1; o < 16; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
         }
-        S.total = acc;
-        if (acc <= cap && acc > 0) {
-            fence_proxy_async_smem();
-            mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 16u * NARR);
-            for (int r = 0; r < R; ++r) {
-                if (!S.rcnt[r]) continue;
-                bulk_g2s(s_buf + S.base[r], a0 + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
-                if (NARR > 1)
-                    bulk_g2s(s_buf + cap + S.base[r], a1 + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+        const uint32_t base = inc - rc, total = __shfl_sync(0xffffffffu, inc, R - 1);
+        if (lane < R) S.base[lane] = base;
+        if (lane == 0) S.total = total;
+        if (total <= cap && total > 0) {
+            if (lane == 0) mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), total * 16u * NARR);
+            __syncwarp();
+            if (lane < R && rc) {
+                fence_proxy_async_smem();
+                bulk_g2s(s_buf + base, a0 + S.lo[lane], rc * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                if (NARR > 1) bulk_g2s(s_buf + cap + base, a1 + S.lo[lane], rc * 16u, reinterpret_cast<uint64_t*>(&S.bar));
             }
         }
     }
@@ -1057,29 +1057,39 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
         const uint32_t tfirst = S.lo[RC] + S.off[RC][1];
         const uint32_t ntarg = S.off[RC][ncell + 1] - S.off[RC][1];
         const bool lists_staged = ntarg <= LIST_STAGE_MAX && S.rcnt[RC] > 0;
-        if (t == 0) {
-            uint32_t acc = 0;
-            for (int r = 0; r < R; ++r) {
-                S.base[r] = acc;
-                acc += S.rcnt[r];
+        // warp 0: row bases (a scan of the rows' counts); if the brick fits, lane 0 arms the
+        // mbarrier with the byte count, lane r copies row r's positions and velocities, and lanes
+        // R .. R + 2 the targets' lists, list lengths and permutation entries
+        if (t < 32) {
+            const uint32_t rc = lane < R ? S.rcnt[lane] : 0u;
+            uint32_t inc = rc;
+#pragma unroll
+            for (int o = 1; o < 16; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
             }
-            S.total = acc;
-            if (acc <= BRICK_CAP && acc > 0) {
+            const uint32_t base = inc - rc, total = __shfl_sync(0xffffffffu, inc, R - 1);
+            if (lane < R) S.base[lane] = base;
+            if (lane == 0) S.total = total;
+            if (total <= BRICK_CAP && total > 0) {
                 const uint32_t lbytes = lists_staged ? ntarg * NBR_CAP * 2 : 0u;
                 // list lengths and permutation entries of the targets, from 16-byte boundaries
                 const uint32_t mbytes = lists_staged ? (((tfirst + ntarg + 1u) & ~1u) - (tfirst & ~1u)) * 8u : 0u;
                 const uint32_t ibytes = lists_staged ? (((tfirst + ntarg + 3u) & ~3u) - (tfirst & ~3u)) * 4u : 0u;
-                fence_proxy_async_smem();
-                mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), acc * 32u + lbytes + mbytes + ibytes);
-                for (int r = 0; r < R; ++r) {
-                    if (!S.rcnt[r]) continue;
-                    bulk_g2s(s_buf + S.base[r], spos + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
-                    bulk_g2s(s_buf + BRICK_CAP + S.base[r], svel + S.lo[r], S.rcnt[r] * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                if (lane == 0)
+                    mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), total * 32u + lbytes + mbytes + ibytes);
+                __syncwarp();
+                uint64_t* bar = reinterpret_cast<uint64_t*>(&S.bar);
+                if (lane < R && rc) {
+                    fence_proxy_async_smem();
+                    bulk_g2s(s_buf + base, spos + S.lo[lane], rc * 16u, bar);
+                    bulk_g2s(s_buf + BRICK_CAP + base, svel + S.lo[lane], rc * 16u, bar);
                 }
-                if (lbytes) {
-                    bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, reinterpret_cast<uint64_t*>(&S.bar));
-                    bulk_g2s(s_meta, nbr_meta + (tfirst & ~1u), mbytes, reinterpret_cast<uint64_t*>(&S.bar));
-                    bulk_g2s(s_index, index + (tfirst & ~3u), ibytes, reinterpret_cast<uint64_t*>(&S.bar));
+                if (lbytes && lane >= R && lane < R + 3) {
+                    fence_proxy_async_smem();
+                    if (lane == R) bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, bar);
+                    else if (lane == R + 1) bulk_g2s(s_meta, nbr_meta + (tfirst & ~1u), mbytes, bar);
+                    else bulk_g2s(s_index, index + (tfirst & ~3u), ibytes, bar);
                 }
             }
         }
