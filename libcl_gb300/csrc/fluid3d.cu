@@ -334,7 +334,10 @@ int st_hash(H* h, const KParams& kp, cudaStream_t s, bool clear) {
     return GBSPH_OK;
 }
 
-int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather, cudaEvent_t before_last = nullptr) {
+// Sorts the keys; with `gather` the last pass also gathers the sorted positions and, with
+// gather_vel, the sorted velocities.
+int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather, cudaEvent_t before_last = nullptr,
+            bool gather_vel = true) {
     OnesweepArgs a;
     a.keys_in = h->keys_a;
     a.vals_in = nullptr;
@@ -350,7 +353,7 @@ int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather, cudaEvent_t be
     a.scratch = h->scratch;
     a.err = h->err;
     if (gather) {
-        a.gather.n_gather = 2;
+        a.gather.n_gather = gather_vel ? 2 : 1;
         a.gather.src[0] = P4(h, 0);
         a.gather.src[1] = P4(h, 1);
         a.gather.dst[0] = h->spos;
@@ -359,6 +362,14 @@ int st_sort(H* h, const KParams& kp, cudaStream_t s, bool gather, cudaEvent_t be
     a.before_last = before_last;
     GBSPH_CUDA_TRY(&h->last_error, onesweep_passes(a, s));
     return GBSPH_OK;
+}
+
+// Sorted velocities gathered on their own (when the velocity upload is still in flight while
+// the sort runs).
+__global__ void k_gather_velocity(const uint32_t* __restrict__ index, const float4* __restrict__ vel,
+                                  float4* __restrict__ svel, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) svel[i] = vel[index[i]];
 }
 
 int st_reorder(H* h, const KParams& kp, cudaStream_t s) {
@@ -533,13 +544,23 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
     if (io) GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[1], 0));
     RC(st_hash(h, kp, s, clear));
     RC(mark(h, 1, s));
-    RC(st_sort(h, kp, s, true, io ? h->io_ev[2] : nullptr));
+    // with host input the sort does not wait for the velocity upload: the sorted velocities
+    // are gathered after the cell bounds (before the density pass, which writes their w)
+    RC(st_sort(h, kp, s, true, nullptr, io == nullptr));
+    auto gather_velocity = [&]() -> int {
+        if (!io) return GBSPH_OK;
+        GBSPH_CUDA_TRY(&h->last_error, cudaStreamWaitEvent(s, h->io_ev[2], 0));
+        k_gather_velocity<<<grid1(kp.n), 256, 0, s>>>(h->index, P4(h, 1), h->svel, kp.n);
+        GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
+        return GBSPH_OK;
+    };
     RC(mark(h, 2, s));
     if (linear) {
         // counters were zeroed with the sort scratch in st_hash
         k_bounds_linear<<<(kp.n + BOUNDS_TILE - 1) / BOUNDS_TILE, 256, 0, s>>>(h->keys_c, kp, h->table, h->bricks, counters(h), h->err);
         GBSPH_CUDA_TRY(&h->last_error, cudaGetLastError());
         h->table_clean = true;
+        RC(gather_velocity());
         RC(mark(h, 3, s));
         RC(st_density_brick(h, kp, s));
         RC(mark(h, 4, s));
@@ -547,6 +568,7 @@ int enqueue_fused(H* h, const KParams& kp, cudaStream_t s, const HostIO* io = nu
         RC(st_force_brick(h, kp, s, h->hook == nullptr));
     } else {
         RC(st_bounds(h, kp, s, true));
+        RC(gather_velocity());
         RC(mark(h, 3, s));
         RC(st_density_exact(h, kp, s, true));
         RC(mark(h, 4, s));
