@@ -983,9 +983,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
-// force_pair on the force pass's staged copies, whose w lanes hold a = 1/rho (positions) and
-// b = p/rho (velocities): (p_i + p_j) / (rho_i rho_j) = b_i a_j + a_i b_j. Skips r = 0 (the
-// target itself, which its list holds, and coincident particles).
+// force_pair on the force pass's staged copies. The target's w lanes hold a_i = 1/rho_i
+// (position) and b_i = p_i/rho_i (velocity); the neighbour's hold rho_j and p_j as the density
+// pass wrote them, from which a_j = rcp(rho_j) and b_j = p_j a_j are formed here:
+// (p_i + p_j) / (rho_i rho_j) = b_i a_j + a_i b_j. Skips r = 0 (the target itself, which its
+// list holds, and coincident particles).
 template <int DIMS>
 __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& vi, const float4& pj,
                                                const float4& vj, float h, float* acc) {
@@ -995,8 +997,9 @@ __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& v
     if (!(r2 > 0.0f)) return;
     const float inv = rsqrtf(r2);
     const float hr = h - r2 * inv;
-    const float dd = pi.w * pj.w;  // 1 / (rho_i rho_j)
-    const float sp = fmaf(vi.w, pj.w, pi.w * vj.w) * (hr * hr * inv);
+    const float aj = rcp_approx(pj.w), bj = vj.w * aj;
+    const float dd = pi.w * aj;  // 1 / (rho_i rho_j)
+    const float sp = fmaf(vi.w, aj, pi.w * bj) * (hr * hr * inv);
     acc[0] = fmaf(sp, dx, acc[0]);
     acc[1] = fmaf(sp, dy, acc[1]);
     acc[2] = fmaf(sp, dz, acc[2]);
@@ -1095,16 +1098,7 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
         }
         __syncthreads();
         const bool staged = S.total <= BRICK_CAP && S.total > 0;
-        if (staged) {
-            if (!brick_wait(S, phase, err)) return false;
-            // w lanes of the staged copies: 1/rho and p/rho (force_pair_pre)
-            for (uint32_t k = t; k < S.total; k += BRICK_THREADS) {
-                const float a = rcp_approx(s_buf[k].w);
-                s_buf[k].w = a;
-                s_buf[BRICK_CAP + k].w *= a;
-            }
-            __syncthreads();
-        }
+        if (staged && !brick_wait(S, phase, err)) return false;
         // P = 2 lanes per target: the brick's targets are consecutive in the centre row, so the
         // CTA takes 128 of them at a time whatever cell they are in; the two lanes of a target
         // split its list (or, in an unstaged brick, take alternate candidates of each row) and
@@ -1131,6 +1125,10 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
                 sub = f >> 8;
                 pi = staged ? s_pos[S.base[RC] + tl] : ld_phase<COH>(spos + gi);
                 vi = staged ? s_vel[S.base[RC] + tl] : ld_phase<COH>(svel + gi);
+                if (staged) {  // the target's w lanes: 1/rho and p/rho (force_pair_pre)
+                    pi.w = rcp_approx(pi.w);
+                    vi.w *= pi.w;
+                }
                 if (p == 0) {  // prefetch what the integration needs
                     o = (staged && lists_staged) ? s_index[gi - (tfirst & ~3u)] : ld_phase<COH>(index + gi);
                     f_o = force[o];
