@@ -55,7 +55,7 @@ static_assert(SORT_MAX_PASSES * SORT_RADIX * 4 <= STEP_SMEM, "hash phase layout"
 template <int ITEMS>
 __global__ void __launch_bounds__(BRICK_THREADS, 3) k_batch_step(BatchStepArgs a, KParams kp) {
     extern __shared__ float4 s_dyn[];
-    __shared__ BrickShared S;
+    __shared__ BrickShared S[2];  // the brick phases use the two records in turn
     __shared__ LaneMap L;
     __shared__ uint32_t s_flag;
     uint32_t* words = reinterpret_cast<uint32_t*>(s_dyn);
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_batch_step(BatchStepArgs a
                                                a.nbr, a.nbr_meta, a.err);
     __syncthreads();
     if (threadIdx.x == 0) {
-        if (ok) mbar_inval(reinterpret_cast<uint64_t*>(&S.bar));  // the force phase initialises it again
+        if (ok) mbar_inval(reinterpret_cast<uint64_t*>(&S[0].bar));  // the force phase initialises it again
         else gs.abort();
     }
     if (!gs.sync(&s_flag)) return;

@@ -646,11 +646,13 @@ __device__ __forceinline__ void brick_setup(BrickShared& S, const KParams& kp, u
 }
 
 // Warp 0: the rows' bases in the staging buffer (a scan of their counts), then, if the brick
-// fits, lane 0 arms the mbarrier with the byte count and lane r copies row r. Returns (to all
-// threads, after a barrier) whether the brick's rows are staged in shared memory.
+// fits, lane 0 arms the mbarrier `bar` with the byte count and lane r copies row r. No barrier:
+// the other warps learn whether the brick is staged from brick_total and wait on `bar`
+// (brick_wait's barrier then publishes the bases).
 template <int DIMS, int NARR>
-__device__ __forceinline__ bool brick_stage(BrickShared& S, float4* s_buf, uint32_t cap,
-                                            const float4* __restrict__ a0, const float4* __restrict__ a1) {
+__device__ __forceinline__ void brick_stage(BrickShared& S, float4* s_buf, uint32_t cap,
+                                            const float4* __restrict__ a0, const float4* __restrict__ a1,
+                                            uint64_t* bar) {
     constexpr int R = DIMS == 3 ? 9 : 3;
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
@@ -663,30 +665,39 @@ __device__ __forceinline__ bool brick_stage(BrickShared& S, float4* s_buf, uint3
         }
         const uint32_t base = inc - rc, total = __shfl_sync(0xffffffffu, inc, R - 1);
         if (lane < R) S.base[lane] = base;
-        if (lane == 0) S.total = total;
         if (total <= cap && total > 0) {
-            if (lane == 0) mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), total * 16u * NARR);
+            if (lane == 0) mbar_arrive_expect_tx(bar, total * 16u * NARR);
             __syncwarp();
             if (lane < R && rc) {
                 fence_proxy_async_smem();
-                bulk_g2s(s_buf + base, a0 + S.lo[lane], rc * 16u, reinterpret_cast<uint64_t*>(&S.bar));
-                if (NARR > 1) bulk_g2s(s_buf + cap + base, a1 + S.lo[lane], rc * 16u, reinterpret_cast<uint64_t*>(&S.bar));
+                bulk_g2s(s_buf + base, a0 + S.lo[lane], rc * 16u, bar);
+                if (NARR > 1) bulk_g2s(s_buf + cap + base, a1 + S.lo[lane], rc * 16u, bar);
             }
         }
     }
-    __syncthreads();
-    return S.total <= cap && S.total > 0;
 }
 
-// Waits for the staged copies. On timeout every thread learns it through S.abort.
-__device__ __forceinline__ bool brick_wait(BrickShared& S, uint32_t& phase, uint32_t* err) {
-    bool ok = mbar_wait_bounded(reinterpret_cast<uint64_t*>(&S.bar), phase);
+// Candidates the brick stages: the sum of its rows' counts (known to every thread after the
+// set-up's barrier).
+template <int DIMS>
+__device__ __forceinline__ uint32_t brick_total(const BrickShared& S) {
+    constexpr int R = DIMS == 3 ? 9 : 3;
+    uint32_t a = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) a += S.rcnt[r];
+    return a;
+}
+
+// Waits for the staged copies (every thread), then a barrier. Returns false to every thread
+// if any thread's wait hit its limit, after draining the copies still in flight (bounded).
+__device__ __forceinline__ bool brick_wait(uint64_t* bar, uint32_t& phase, uint32_t* err) {
+    bool ok = mbar_wait_bounded(bar, phase);
     if (!ok) atomicOr(err, DEV_ERR_MBAR_TIMEOUT);
     ok = __syncthreads_and(ok);
     phase ^= 1u;
     if (!ok && threadIdx.x == 0) {
         // drain the copies still in flight (bounded) before this CTA's shared memory goes away
-        mbar_wait_bounded(reinterpret_cast<uint64_t*>(&S.bar), phase ^ 1u);
+        mbar_wait_bounded(bar, phase ^ 1u);
     }
     return ok;
 }
@@ -771,10 +782,12 @@ __device__ __forceinline__ void lane_map_init(LaneMap& L) {
 typedef uint8_t SubListCounts[BRICK_WARPS][GROUP_MAX][NBR_SUBLISTS];  // sub-list lengths per warp group
 
 // The body of k_density_brick, on shared memory the caller provides: s_buf (DENSITY_SMEM
-// bytes), S, L and wcnt. The batched step's persistent kernel runs it as one of its phases.
-// Returns false if a bulk-copy wait gave up (the CTA left the loop).
+// bytes), S2 (two brick records, used in turn, so that a warp may start the next brick's
+// set-up while others still compute this one), L and wcnt. The batched step's persistent
+// kernel runs it as one of its phases. Returns false if a bulk-copy wait gave up (the CTA left
+// the loop).
 template <int DIMS, bool BATCH>
-__device__ __forceinline__ bool density_brick_run(float4* s_buf, BrickShared& S, LaneMap& L, SubListCounts& wcnt,
+__device__ __forceinline__ bool density_brick_run(float4* s_buf, BrickShared* S2, LaneMap& L, SubListCounts& wcnt,
                                                   float4* __restrict__ spos, float4* __restrict__ svel,
                                                   const uint2* __restrict__ table, const uint32_t* __restrict__ bricks,
                                                   uint32_t* counters, const KParams& kp, uint16_t* __restrict__ nbr,
@@ -784,26 +797,31 @@ __device__ __forceinline__ bool density_brick_run(float4* s_buf, BrickShared& S,
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     uint16_t* wlist = reinterpret_cast<uint16_t*>(s_buf + BRICK_CAP) + warp * GROUP_MAX * WLIST_STRIDE;
     lane_map_init(L);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(&S2[0].bar);
     if (t == 0) {
-        mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
+        mbar_init(bar, 1);
         fence_mbar_init();
     }
     uint32_t phase = 0;
     const uint32_t n_bricks = __ldcg(counters);  // written by the bounds pass (an earlier kernel or phase)
     const float h2 = kp.h2, thr = kp.r2_thresh;
     const uint32_t buf_a = smem_addr(s_buf);
-    // the next brick's id is fetched while this one is processed
-    if (t == 0) S.brick = atomicAdd(&counters[1], 1u);
-    for (;;) {
-        __syncthreads();
+    // Brick k uses record S2[k & 1]. Its id was fetched at the start of brick k - 1 and is read
+    // after that brick's barriers; the set-up's barrier of brick k (all warps are done with
+    // brick k - 1) comes before the copies into the staging buffer.
+    if (t == 0) S2[0].brick = atomicAdd(&counters[1], 1u);
+    __syncthreads();
+    for (uint32_t it = 0;; it ^= 1u) {
+        BrickShared& S = S2[it];
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
-        uint32_t next_brick = 0;
-        if (t == 0) next_brick = atomicAdd(&counters[1], 1u);
+        if (t == 0) S2[it ^ 1u].brick = atomicAdd(&counters[1], 1u);
         int x0, ncell;
         brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
-        const bool staged = brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr);
-        if (staged && !brick_wait(S, phase, err)) return false;
+        brick_stage<DIMS, 1>(S, s_buf, BRICK_CAP, spos, nullptr, bar);
+        const uint32_t total = brick_total<DIMS>(S);
+        const bool staged = total <= BRICK_CAP && total > 0;
+        if (staged && !brick_wait(bar, phase, err)) return false;
         for (int c = warp; c < ncell; c += BRICK_WARPS) {
             const uint32_t t0 = S.off[RC][c + 1], nt = S.off[RC][c + 2] - t0;
             for (uint32_t g0 = 0; g0 < nt; g0 += GROUP_MAX) {
@@ -935,7 +953,6 @@ __device__ __forceinline__ bool density_brick_run(float4* s_buf, BrickShared& S,
                 __syncwarp();
             }
         }
-        if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
     }
     return true;
 }
@@ -949,7 +966,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 4) k_density_brick(float4* __re
                                                                  uint16_t* __restrict__ nbr,
                                                                  uint64_t* __restrict__ nbr_meta, uint32_t* err) {
     extern __shared__ float4 s_buf[];  // [BRICK_CAP] positions, then per-warp neighbour lists
-    __shared__ BrickShared S;
+    __shared__ BrickShared S[2];
     __shared__ LaneMap L;
     __shared__ __align__(8) SubListCounts wcnt;
     density_brick_run<DIMS, BATCH>(s_buf, S, L, wcnt, spos, svel, table, bricks, counters, kp, nbr, nbr_meta, err);
@@ -1023,7 +1040,7 @@ __device__ __forceinline__ void force_pair_pre(const float4& pi, const float4& v
 // in the same launch, so the direct loads of them go through L2 only. Returns false if a
 // bulk-copy wait gave up (the CTA left the loop).
 template <int DIMS, bool FUSED, bool BATCH, bool COH = false>
-__device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, LaneMap& L,
+__device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared* S2, LaneMap& L,
                                                 const float4* __restrict__ spos, const float4* __restrict__ svel,
                                                 const uint32_t* __restrict__ index, float4* __restrict__ pos,
                                                 float4* __restrict__ vel, float4* __restrict__ force,
@@ -1035,8 +1052,9 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
     constexpr int RC = DIMS == 3 ? 4 : 1;
     const int t = threadIdx.x, lane = t & 31;
     lane_map_init(L);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(&S2[0].bar);
     if (t == 0) {
-        mbar_init(reinterpret_cast<uint64_t*>(&S.bar), 1);
+        mbar_init(bar, 1);
         fence_mbar_init();
     }
     uint32_t phase = 0;
@@ -1046,14 +1064,14 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
     uint16_t* s_lists = reinterpret_cast<uint16_t*>(s_buf + 2 * BRICK_CAP);
     uint64_t* s_meta = reinterpret_cast<uint64_t*>(reinterpret_cast<char*>(s_lists) + FORCE_LIST_BYTES);
     uint32_t* s_index = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(s_meta) + FORCE_META_BYTES);
-    // the next brick's id is fetched while this one is processed
-    if (t == 0) S.brick = atomicAdd(&counters[2], 1u);
-    for (;;) {
-        __syncthreads();
+    // records used in turn, as in density_brick_run
+    if (t == 0) S2[0].brick = atomicAdd(&counters[2], 1u);
+    __syncthreads();
+    for (uint32_t it = 0;; it ^= 1u) {
+        BrickShared& S = S2[it];
         const uint32_t b = S.brick;
         if (b >= n_bricks) break;
-        uint32_t next_brick = 0;
-        if (t == 0) next_brick = atomicAdd(&counters[2], 1u);
+        if (t == 0) S2[it ^ 1u].brick = atomicAdd(&counters[2], 1u);
         int x0, ncell;
         brick_setup<DIMS, BATCH>(S, kp, bricks[b], table, err, x0, ncell);
         // the brick's targets are consecutive particles: stage their lists with the rows
@@ -1073,16 +1091,13 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
             }
             const uint32_t base = inc - rc, total = __shfl_sync(0xffffffffu, inc, R - 1);
             if (lane < R) S.base[lane] = base;
-            if (lane == 0) S.total = total;
             if (total <= BRICK_CAP && total > 0) {
                 const uint32_t lbytes = lists_staged ? ntarg * NBR_CAP * 2 : 0u;
                 // list lengths and permutation entries of the targets, from 16-byte boundaries
                 const uint32_t mbytes = lists_staged ? (((tfirst + ntarg + 1u) & ~1u) - (tfirst & ~1u)) * 8u : 0u;
                 const uint32_t ibytes = lists_staged ? (((tfirst + ntarg + 3u) & ~3u) - (tfirst & ~3u)) * 4u : 0u;
-                if (lane == 0)
-                    mbar_arrive_expect_tx(reinterpret_cast<uint64_t*>(&S.bar), total * 32u + lbytes + mbytes + ibytes);
+                if (lane == 0) mbar_arrive_expect_tx(bar, total * 32u + lbytes + mbytes + ibytes);
                 __syncwarp();
-                uint64_t* bar = reinterpret_cast<uint64_t*>(&S.bar);
                 if (lane < R && rc) {
                     fence_proxy_async_smem();
                     bulk_g2s(s_buf + base, spos + S.lo[lane], rc * 16u, bar);
@@ -1096,9 +1111,9 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
                 }
             }
         }
-        __syncthreads();
-        const bool staged = S.total <= BRICK_CAP && S.total > 0;
-        if (staged && !brick_wait(S, phase, err)) return false;
+        const uint32_t total = brick_total<DIMS>(S);
+        const bool staged = total <= BRICK_CAP && total > 0;
+        if (staged && !brick_wait(bar, phase, err)) return false;
         // P = 2 lanes per target: the brick's targets are consecutive in the centre row, so the
         // CTA takes 128 of them at a time whatever cell they are in; the two lanes of a target
         // split its list (or, in an unstaged brick, take alternate candidates of each row) and
@@ -1288,7 +1303,7 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared& S, L
                 }
             }
         }
-        if (t == 0) S.brick = next_brick;  // read by every thread after the barrier at the top
+        __syncthreads();  // every warp is done with the brick before the next one's set-up
     }
     return true;
 }
@@ -1307,7 +1322,7 @@ __global__ void __launch_bounds__(BRICK_THREADS, 3) k_force_brick(const float4* 
                                                                const uint64_t* __restrict__ nbr_meta,
                                                                uint32_t* err) {
     extern __shared__ float4 s_buf[];
-    __shared__ BrickShared S;
+    __shared__ BrickShared S[2];
     __shared__ LaneMap L;
     force_brick_run<DIMS, FUSED, BATCH>(s_buf, S, L, spos, svel, index, pos, vel, force, table, bricks, counters, kp,
                                         nbr, nbr_meta, err);
