@@ -387,13 +387,12 @@ __global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__
     if (particle >= kp.n) return;
     const float4 posI = spos[particle], velI = svel[particle];
     float px = 0.f, py = 0.f, pz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;
-    auto pair = [&](uint32_t j) {
-        const float4 posJ = spos[j];
+    // one pair with the neighbour's position and velocity at hand
+    auto pair_at = [&](const float4& posJ, const float4& velJ) {
         const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
         const float r2 = exact_r2(vx, vy, vz);
         if (r2 < kp.r2_thresh) {  // fast_length < h
             const float vlen = __fsqrt_rn(r2);
-            const float4 velJ = svel[j];
             const float density2 = __fmul_rn(posI.w, posJ.w);
             const float s = __fdiv_rn(__fadd_rn(velI.w, velJ.w), density2);
             const float hr = __fsub_rn(kp.h, vlen);
@@ -405,9 +404,31 @@ __global__ void __launch_bounds__(256) k_forces_exact(const float4* __restrict__
             qz = __fadd_rn(qz, __fmul_rn(__fdiv_rn(__fsub_rn(velJ.z, velI.z), density2), hr));
         }
     };
+    auto pair = [&](uint32_t j) {
+        const float4 posJ = spos[j];
+        const float vx = __fsub_rn(posI.x, posJ.x), vy = __fsub_rn(posI.y, posJ.y), vz = __fsub_rn(posI.z, posJ.z);
+        if (exact_r2(vx, vy, vz) < kp.r2_thresh) pair_at(posJ, svel[j]);
+    };
     const uint32_t nl = LISTED ? xc[particle] : EMPTY;
     if (LISTED && nl <= XL_CAP) {
-        for (uint32_t k = 0; k < nl; ++k) pair(xl[(size_t)k * kp.n + particle]);
+        // the recorded neighbours in their order; the next one's index, position and velocity
+        // are loaded while the current pair is computed
+        const uint32_t* mine = xl + particle;
+        float4 pn = posI, vn = velI;
+        if (nl) {
+            const uint32_t j0 = mine[0];
+            pn = spos[j0];
+            vn = svel[j0];
+        }
+        for (uint32_t k = 0; k < nl; ++k) {
+            const float4 posJ = pn, velJ = vn;
+            if (k + 1 < nl) {
+                const uint32_t jn = mine[(size_t)(k + 1) * kp.n];
+                pn = spos[jn];
+                vn = svel[jn];
+            }
+            pair_at(posJ, velJ);
+        }
     } else {
         for_each_neighbour_cell<MODE>(kp, tab, posI, [&](uint32_t start, uint32_t end) {
             for (uint32_t j = start; j < end; j++)
