@@ -225,3 +225,53 @@ def test_full_ensemble_against_oracle_and_scenes_run_alone(cuda):
             assert rel_err(got["vel"][a:a + n], vel) <= RTOL, (s, "velocity")
             assert pos_err(got["pos"][a:a + n], pos, sc.pos) <= 1.0, (s, "position")
             assert np.array_equal(got["force"][a:a + n], force), (s, "force (gravity seed)")
+
+
+def _dense_clump_batch():
+    """Four scenes: two ordinary lattice blocks, one whose 2,500 particles sit inside a single
+    cell (its brick stages more candidates than fit, so both neighbour passes read global
+    memory and every target overflows its lists), and one with a quarter of its particles
+    beyond its grid on every side (clamped into the border cells)."""
+    b = batched_ensemble(n_scenes=4, seed=41, n_min=2000, n_max=6000)
+    rng = np.random.default_rng(12)
+    a, n = b.firsts[2], b.descs[2].n_particles
+    h = float(b.shared.cellSize)
+    b.pos[a:a + n, :3] = (h * (3.0 + rng.uniform(0.05, 0.95, (n, 3)))).astype(np.float32)
+    a, n = b.firsts[3], b.descs[3].n_particles
+    far = rng.random(n) < 0.25
+    ext = np.array([b.descs[3].gridDim[i] * h for i in range(3)], np.float32)
+    b.pos[a:a + n, :3][far] = (ext * rng.choice([-0.3, 1.3], (int(far.sum()), 3))).astype(np.float32)
+    b.vel[:, :3] = rng.normal(0, 0.05, (b.n, 3)).astype(np.float32)
+    return b
+
+
+def test_persistent_step_matches_staged_on_clumps_and_clamped_particles(cuda):
+    b = _dense_clump_batch()
+    ref = _run_batch(b, 3, 0, bw=8)
+    got = _run_batch(b, 3, 1, bw=8)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+def test_persistent_step_on_tiny_scenes(cuda):
+    """Scenes of 8 to 30 particles (one sort tile, a few bricks, most CTAs of the cooperative
+    grid without work): persistent equals staged, and both leave no device error."""
+    b = batched_ensemble(n_scenes=3, seed=2, n_min=8, n_max=30)
+    ref = _run_batch(b, 5, 0)
+    got = _run_batch(b, 5, 1)
+    for w in ALL_BUFFERS:
+        assert np.array_equal(ref[w], got[w]), w
+
+
+def test_persistent_step_is_captured_in_a_graph(cuda):
+    """On this driver the cooperative launch is captured into the step's graph (a refused
+    capture would run eagerly and say so in the handle's last error)."""
+    import torch
+    b = batched_ensemble(n_scenes=3, seed=1, n_min=1000, n_max=2000)
+    bt = load_batch(b)
+    bt.set_option(OPT_PERSISTENT, 1)
+    for _ in range(3):
+        bt.compute()
+    torch.cuda.synchronize()
+    assert bt.sync_status() == 0
+    assert bt._lib.gbsph_batch3d_last_error(bt._h).decode() == ""
