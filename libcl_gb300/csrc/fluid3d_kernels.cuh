@@ -690,7 +690,10 @@ __device__ __forceinline__ void brick_stage(BrickShared& S, float4* s_buf, uint3
             if (lane == 0) mbar_arrive_expect_tx(bar, total * 16u * NARR);
             __syncwarp();
             if (lane < R && rc) {
+                // this lane's generic-proxy accesses (shared memory, and global memory that an
+                // earlier phase of a persistent kernel wrote) before its bulk copies
                 fence_proxy_async_smem();
+                fence_proxy_async_global();
                 bulk_g2s(s_buf + base, a0 + S.lo[lane], rc * 16u, bar);
                 if (NARR > 1) bulk_g2s(s_buf + cap + base, a1 + S.lo[lane], rc * 16u, bar);
             }
@@ -1120,12 +1123,14 @@ __device__ __forceinline__ bool force_brick_run(float4* s_buf, BrickShared* S2, 
                 if (lane == 0) mbar_arrive_expect_tx(bar, total * 32u + lbytes + mbytes + ibytes);
                 __syncwarp();
                 if (lane < R && rc) {
-                    fence_proxy_async_smem();
+                    fence_proxy_async_smem();  // as in brick_stage
+                    fence_proxy_async_global();
                     bulk_g2s(s_buf + base, spos + S.lo[lane], rc * 16u, bar);
                     bulk_g2s(s_buf + BRICK_CAP + base, svel + S.lo[lane], rc * 16u, bar);
                 }
                 if (lbytes && lane >= R && lane < R + 3) {
                     fence_proxy_async_smem();
+                    fence_proxy_async_global();
                     if (lane == R) bulk_g2s(s_lists, nbr + (size_t)tfirst * NBR_CAP, lbytes, bar);
                     else if (lane == R + 1) bulk_g2s(s_meta, nbr_meta + (tfirst & ~1u), mbytes, bar);
                     else bulk_g2s(s_index, index + (tfirst & ~3u), ibytes, bar);

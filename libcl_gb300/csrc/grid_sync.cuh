@@ -50,7 +50,7 @@ struct GridSync {
                 }
             }
             __threadfence();
-            fence_proxy_async_global();  // bulk copies thread 0 issues next see the writes
+            fence_proxy_async_global();  // bulk copies issued after the barrier see the writes
             if (ld_relaxed_gpu(w + 2)) ok = false;
             *s_flag = ok ? 1u : 0u;
         }
