@@ -565,11 +565,9 @@ static __global__ void k_post_fused(const float4* __restrict__ spos, const float
 struct BrickShared {
     uint32_t off[9][BRICK_SLOTS + 1];  // lower bounds of each cell inside the row's range
     uint32_t lo[9];                    // first sorted index of the row's range
-    uint32_t rcnt[9];
+    uint32_t rcnt[9];                  // candidates of the row
     uint32_t base[9];                  // offset of the row in the staging buffer
-    uint32_t total;
-    uint32_t brick;
-    uint32_t abort;
+    uint32_t brick;                    // index into the occupied-brick list
     // the brick's scene: grid, cell-table offset and the parameters that vary per scene
     int nx, ny, nz, bxn;
     uint32_t cell_off, lbrick;  // lbrick: the brick's id within its scene
