@@ -2,7 +2,8 @@
 
 ctypes bindings to oracle/_ref/libclref.so, which oracle/ref/build.py compiles from the
 reference's OpenCL C sources (libCL/phys/oclFluid3D.cl, libCL/phys/oclFluid2D.cl,
-libCL/sort/oclRadixSort.cl) through an OpenCL C shim (oracle/ref/clshim.h). Each entry point
+libCL/sort/oclRadixSort.cl, libCL/geom/oclBvhTrimesh.cl, libCL/geom/oclBvhLines.cl) through an
+OpenCL C shim (oracle/ref/clshim.h). Each entry point
 enqueues the kernels in the order the reference's host class does. Used by the tests to pin
 the oracle restatement (oracle/*.cpp) to the reference, and by bench.py's reference arm as
 the reference's CPU implementation of the step. The product library never loads it.
@@ -51,6 +52,8 @@ def _load():
         "clref2d_compute_border": (None, [P, I, I, P, P, P]),
         "clref2d_step": (I, [P, U, P, P, P, I, I, P, P, P, P, P, P, P, P]),
         "clref2d_emit": (None, [P, U, U, P]),
+        "clref_bvh_build": (I, [P, U, P, U, P, P, P, P, P]),
+        "clref_bvh_lines_build": (I, [P, U, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -198,3 +201,37 @@ def step_2d(state: np.ndarray, params, border_state: np.ndarray, border_vec: np.
 
 def emit2d(state: np.ndarray, emit: int, params) -> None:
     lib().clref2d_emit(_p(state), state.shape[0], emit, C.addressof(params))
+
+
+def bvh_build(vertex: np.ndarray, index: np.ndarray, box: np.ndarray, root: int = 0):
+    """oclBvhTrimesh::compute through the reference's kernels: vertex float32 [V, 4], index
+    uint32 [3 n], box float32 [8] updated in place (bfAABB, kept across builds). Returns (rc,
+    nodes [2n - 1], root, sorted keys, sorted triangle ids); rc -5 means two Morton keys are
+    equal (the reference's linking races on them) and nothing else is returned."""
+    from oracle import BVH_NODE_DTYPE
+    vertex = np.ascontiguousarray(vertex, np.float32)
+    index = np.ascontiguousarray(index, np.uint32)
+    n = index.size // 3
+    nodes = np.zeros(2 * n - 1, BVH_NODE_DTYPE)
+    r = np.array([root], np.uint32)
+    sk = np.empty(n, np.uint32)
+    sv = np.empty(n, np.uint32)
+    rc = int(lib().clref_bvh_build(_p(vertex), vertex.shape[0], _p(index), n, _p(box), _p(nodes), _p(r), _p(sk),
+                                   _p(sv)))
+    return rc, nodes, int(r[0]), sk, sv
+
+
+def bvh_lines_build(vertex: np.ndarray, root: int = 0):
+    """oclBvhLines::compute through the reference's kernels on float32 [V, 2] (two vertices per
+    segment). Returns (rc, nodes [2n - 1], root, sorted keys, sorted segment ids), rc as in
+    bvh_build."""
+    from oracle import BVH2D_NODE_DTYPE
+    vertex = np.ascontiguousarray(vertex, np.float32)
+    n = vertex.shape[0] // 2
+    vertex = np.ascontiguousarray(vertex[:2 * n])
+    nodes = np.zeros(2 * n - 1, BVH2D_NODE_DTYPE)
+    r = np.array([root], np.uint32)
+    sk = np.empty(n, np.uint32)
+    sv = np.empty(n, np.uint32)
+    rc = int(lib().clref_bvh_lines_build(_p(vertex), n, _p(nodes), _p(r), _p(sk), _p(sv)))
+    return rc, nodes, int(r[0]), sk, sv

@@ -2,14 +2,15 @@
 
     python -m oracle.ref.build [--force]
 
-1. Reads libCL/phys/oclFluid3D.cl, libCL/phys/oclFluid2D.cl and libCL/sort/oclRadixSort.cl
-   from the reference checkout (LIBCL_REFERENCE, default /root/reference) and writes their
-   C++ translations (oracle/ref/rewrite.py: comments blanked, vector literals, __local,
-   barrier kernels as coroutines) to oracle/_ref/gen/. Nothing from the reference is
+1. Reads libCL/phys/oclFluid3D.cl, libCL/phys/oclFluid2D.cl, libCL/sort/oclRadixSort.cl,
+   libCL/geom/oclBvhTrimesh.cl and libCL/geom/oclBvhLines.cl from the reference checkout
+   (LIBCL_REFERENCE, default /root/reference) and writes their C++ translations
+   (oracle/ref/rewrite.py: comments blanked, vector literals, __local, barrier kernels as
+   coroutines, lockstep butterfly steps) to oracle/_ref/gen/. Nothing from the reference is
    copied into the repository: oracle/_ref/ is git-ignored.
 2. Compiles the translations with the shim (oracle/ref/clshim.h) and the drivers
-   (oracle/ref/ref3d.cpp, ref2d.cpp, refsort.cpp, which enqueue the kernels as the
-   reference's host classes do) into oracle/_ref/libclref.so with g++ (C++20, OpenMP,
+   (oracle/ref/ref3d.cpp, ref2d.cpp, refsort.cpp, refbvh.cpp, which enqueue the kernels as
+   the reference's host classes do) into oracle/_ref/libclref.so with g++ (C++20, OpenMP,
    -ffp-contract=off so that x86 and Arm give the same bits).
 
 Where the reference checkout is absent (a machine that only received a copy of this tree),
@@ -32,8 +33,10 @@ SOURCES = {
     "oclFluid3D.cl.inc": "phys/oclFluid3D.cl",
     "oclFluid2D.cl.inc": "phys/oclFluid2D.cl",
     "oclRadixSort.cl.inc": "sort/oclRadixSort.cl",
+    "oclBvhTrimesh.cl.inc": "geom/oclBvhTrimesh.cl",
+    "oclBvhLines.cl.inc": "geom/oclBvhLines.cl",
 }
-DRIVERS = ["ref3d.cpp", "ref2d.cpp", "refsort.cpp"]
+DRIVERS = ["ref3d.cpp", "ref2d.cpp", "refsort.cpp", "refbvh.cpp"]
 
 
 def generate() -> bool:

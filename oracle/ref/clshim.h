@@ -1,6 +1,7 @@
 // clshim.h -- a small OpenCL C 1.1 environment for C++20, so that the reference's own
 // kernel sources (libCL/phys/oclFluid3D.cl, libCL/phys/oclFluid2D.cl,
-// libCL/sort/oclRadixSort.cl) compile and run on the host cores.
+// libCL/sort/oclRadixSort.cl, libCL/geom/oclBvhTrimesh.cl, libCL/geom/oclBvhLines.cl) compile
+// and run on the host cores.
 //
 // TEST INFRASTRUCTURE ONLY: it exists to execute the reference's kernels as the checker of
 // the oracle restatement (and, through it, of the CUDA library). Nothing in the product
@@ -34,14 +35,17 @@
 //     i0 = floor(u), a = u - floor(u), CLK_ADDRESS_CLAMP_TO_EDGE clamps the texel indices,
 //     T = (1-a)(1-b)T00 + a(1-b)T10 + (1-a)bT01 + abT11 summed left to right), and
 //     write_imagef rounding to half precision to nearest even;
+//   * atom_cmpxchg on int and uint words (a sequentially consistent compare-and-swap);
 //   * barrier(): kernels that call it are compiled as C++20 coroutines (the source rewrite
 //     turns barrier(...) into `co_await clc::barrier_point{}` and `return;` into
 //     `co_return;`); run_groups_coro() runs a work-group's work-items in local-id order up
 //     to each barrier in turn, which is what the barrier requires of a work-group. __local
 //     arrays declared in a kernel body live in per-host-thread storage (local_array), shared
 //     by the work-group the thread is running.
-// Work-groups of one launch run on OpenMP threads; the reference's kernels write disjoint
-// locations per work-item, so the results do not depend on the schedule.
+// Work-groups of one launch run on OpenMP threads where the reference's kernels write disjoint
+// locations per work-item, so that the results do not depend on the schedule; the runners'
+// PAR = false runs a launch's work-groups one after another on the calling thread (for the
+// kernels whose work-items meet through atomics).
 #pragma once
 
 #include <cmath>
@@ -49,6 +53,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <atomic>
 #include <exception>
 #include <type_traits>
 #include <vector>
@@ -66,8 +71,9 @@
 #define __write_only
 #define CLK_LOCAL_MEM_FENCE 1u
 #define CLK_GLOBAL_MEM_FENCE 2u
-// OpenCL C's predefined float constant (the float nearest to pi).
+// OpenCL C's predefined float constants (the float nearest to pi; the largest finite float).
 #define M_PI_F 3.14159274101257f
+#define MAXFLOAT 3.40282346638528859811704183484516925e+38F
 
 namespace clc {
 
@@ -329,12 +335,13 @@ inline void set_local_id(work_item& w, size_t l) {
     w.gid[0] = w.grp[0] * w.lsize[0] + l;
 }
 
-// A kernel without barriers: every work-item of a 1D range, groups on OpenMP threads.
-// `global` must be a multiple of `local` (the reference's OpenCL 1.x launches are).
-template <class F>
+// A kernel without barriers: every work-item of a 1D range, groups on OpenMP threads (PAR) or
+// in order on the calling thread. `global` must be a multiple of `local` (the reference's
+// OpenCL 1.x launches are).
+template <bool PAR = true, class F>
 inline void run_groups(size_t global, size_t local, F&& f) {
     const long long groups = (long long)(global / local);
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(dynamic, 4) if (PAR)
     for (long long g = 0; g < groups; g++) {
         work_item& w = enter_group_1d(global, local, (size_t)g);
         for (size_t l = 0; l < local; l++) {
@@ -421,10 +428,10 @@ struct barrier_point {
 // A kernel with barriers: each work-group's items start in local-id order and run to their
 // first barrier, then are resumed in the same order, one barrier interval at a time.
 // `local_mem(bytes)` returns the group's __local argument buffers (sized by the caller).
-template <class F>
+template <bool PAR = true, class F>
 inline void run_groups_coro(size_t global, size_t local, F&& f) {
     const long long groups = (long long)(global / local);
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(dynamic, 4) if (PAR)
     for (long long g = 0; g < groups; g++) {
         std::vector<wi_task> items(local);
         work_item& w = enter_group_1d(global, local, (size_t)g);
@@ -443,6 +450,21 @@ inline void run_groups_coro(size_t global, size_t local, F&& f) {
         }
         for (auto& t : items) t.h.destroy();
     }
+}
+
+// ------------------------------------------------------------------------------------
+// Atomics
+// ------------------------------------------------------------------------------------
+// atom_cmpxchg(p, cmp, val): stores val if *p == cmp; returns the old *p.
+template <class T, class = std::enable_if_t<std::is_same_v<T, int> || std::is_same_v<T, uint>>>
+inline T atom_cmpxchg(T* p, T cmp, T val) {
+    std::atomic_ref<T> a(*p);
+    a.compare_exchange_strong(cmp, val);
+    return cmp;
+}
+template <class T, class C, class V, class = std::enable_if_t<std::is_same_v<T, int> || std::is_same_v<T, uint>>>
+inline T atom_cmpxchg(T* p, C cmp, V val) {
+    return atom_cmpxchg<T>(p, (T)cmp, (T)val);
 }
 
 // ------------------------------------------------------------------------------------

@@ -17,7 +17,14 @@ own lines through a #line directive):
    body becomes `static thread_local`;
 4. a kernel whose body calls barrier() becomes a coroutine: its return type `void` becomes
    `clc::wi_task`, `barrier(...);` becomes `co_await clc::barrier_point{};` and `return;`
-   becomes `co_return;`.
+   becomes `co_return;`;
+5. in such a kernel, a statement at the top level of the body of the form
+   `a[lid] = min(a[lid], a[lid ^ k]);` (or max) -- a butterfly step that reads another
+   work-item's __local element with no barrier in between, relying on the work-group being
+   one 32-wide warp executing each statement in lockstep (clAABB in
+   libCL/geom/oclBvhTrimesh.cl:53-60, launched with a local size of 32, cWarpSize in
+   libCL/geom/oclBvhTrimesh.cpp:18,87) -- gets a barrier appended on its line, so that the
+   host runs the statement for every work-item before the next one, as the warp does.
 """
 from __future__ import annotations
 
@@ -27,6 +34,7 @@ _VEC_LITERAL = re.compile(r"\(\s*(float|int|uint)(2|4)\s*\)\s*\(")
 _BARRIER = re.compile(r"\bbarrier\s*\([^;]*\)\s*;")
 _RETURN = re.compile(r"\breturn\s*;")
 _KERNEL = re.compile(r"__kernel\s+void\s+\w+\s*\(")
+_BUTTERFLY = re.compile(r"^\s*(\w+)\[(\w+)\]\s*=\s*(min|max)\(\s*\1\[\2\]\s*,\s*\1\[\2\s*\^\s*\d+\]\s*\)\s*;\s*$")
 
 
 def blank_comments(src: str) -> str:
@@ -104,6 +112,19 @@ def _locals(src: str) -> str:
     return "".join(out)
 
 
+def _lockstep(body: str) -> str:
+    """Rule 5: a barrier after each butterfly statement at the body's top level (brace depth
+    1 of the body, which starts at its opening brace)."""
+    out = []
+    depth = 0
+    for line in body.split("\n"):
+        if depth == 1 and _BUTTERFLY.match(line):
+            line = line + " barrier(CLK_LOCAL_MEM_FENCE);"
+        depth += line.count("{") - line.count("}")
+        out.append(line)
+    return "\n".join(out)
+
+
 def _coroutines(src: str) -> tuple[str, list[str]]:
     out = []
     names = []
@@ -120,6 +141,7 @@ def _coroutines(src: str) -> tuple[str, list[str]]:
         if _BARRIER.search(body):
             name = re.match(r"__kernel\s+void\s+(\w+)", header).group(1)
             names.append(name)
+            body = _lockstep(body)
             header = re.sub(r"__kernel\s+void", "clc::wi_task", header, count=1)
             body = _BARRIER.sub("co_await clc::barrier_point{};", body)
             body = _RETURN.sub("co_return;", body)

@@ -1,13 +1,15 @@
 """Pins the oracle restatement to the reference's own kernels (CPU).
 
 oracle/ref/build.py compiles the reference's OpenCL C sources (libCL/phys/oclFluid3D.cl,
-libCL/phys/oclFluid2D.cl, libCL/sort/oclRadixSort.cl) for the host cores through the shim
-oracle/ref/clshim.h, and oracle/ref/*.cpp enqueue them as the reference's host classes do
-(oclFluid3D::compute, oclFluid2D::compute and computeBorder, oclRadixSort::compute). Each
-test here runs those kernels and the oracle (oracle/*.cpp) on the same inputs and requires
-the same bits: sort, keys, permutation, cell bounds, densities, pressures, forces, positions,
-velocities, wall images, parameter defaults, emitters and the BVH collision. The GPU tests
-compare the CUDA library with the oracle, so they inherit this pin.
+libCL/phys/oclFluid2D.cl, libCL/sort/oclRadixSort.cl, libCL/geom/oclBvhTrimesh.cl,
+libCL/geom/oclBvhLines.cl) for the host cores through the shim oracle/ref/clshim.h, and
+oracle/ref/*.cpp enqueue them as the reference's host classes do (oclFluid3D::compute,
+oclFluid2D::compute and computeBorder, oclRadixSort::compute, oclBvhTrimesh::compute,
+oclBvhLines::compute). Each test here runs those kernels and the oracle (oracle/*.cpp) on the
+same inputs and requires the same bits: sort, keys, permutation, cell bounds, densities,
+pressures, forces, positions, velocities, wall images, parameter defaults, emitters, the BVH
+builds and the BVH collision. The GPU tests compare the CUDA library with the oracle, so
+they inherit this pin.
 
 The shim fixes what OpenCL leaves to the implementation as the oracle does (fast_length and
 length as sqrtf of the left-to-right sum of squares, IEEE division, pow(x, 3.0f) as x*x*x);
@@ -238,6 +240,72 @@ def test_collide_bvh_matches_the_reference():
     assert_same_bits(b[1], a[2], "velocities")
     assert_same_bits(b[2], a[0], "forces")
     assert np.all(a[2] == 0, axis=1).sum() > n // 2
+
+
+# ---------------------------------------------------------------------------------------
+# BVH builds (libCL/geom/oclBvhTrimesh.cl, oclBvhTrimesh::compute; libCL/geom/oclBvhLines.cl,
+# oclBvhLines::compute)
+# ---------------------------------------------------------------------------------------
+def _same_build(o, r, what):
+    nodes_o, root_o, sk_o, sv_o = o
+    rc, nodes_r, root_r, sk_r, sv_r = r
+    assert rc == 0, rc
+    assert root_o == root_r, (root_o, root_r)
+    np.testing.assert_array_equal(sk_o, sk_r, err_msg=f"{what}: sorted Morton keys")
+    np.testing.assert_array_equal(sv_o, sv_r, err_msg=f"{what}: sorted ids")
+    assert_same_bits(nodes_o.view(np.uint32), nodes_r.view(np.uint32), f"{what}: nodes")
+
+
+@pytest.mark.parametrize("mesh", ["soup", "sphere", "around_origin"])
+def test_bvh_build_matches_the_reference(mesh):
+    """Global box (clAABB), Morton keys, the reference's radix sort, node creation, linking,
+    leaves and the bottom-up boxes: every node's 48 bytes, the root and the box."""
+    from libcl_gb300.scenes import triangle_soup
+    if mesh == "soup":
+        v, idx = triangle_soup(3000)
+    elif mesh == "sphere":
+        v, idx = sphere_mesh(24, 48)
+    else:  # a soup that straddles the origin (negative coordinates in every axis)
+        v, idx = triangle_soup(2000, seed=9)
+        v[:, :3] -= np.array([0.8, 0.3, 0.6], np.float32)
+    box_o, box_r = np.zeros(8, np.float32), np.zeros(8, np.float32)
+    _same_build(oracle.bvh_build(v, idx, box_o), ref.bvh_build(v, idx, box_r), mesh)
+    assert_same_bits(box_o, box_r, "global box")
+
+
+def test_bvh_box_and_root_persist_across_builds_as_the_reference():
+    """bfAABB and mRootNode are kept between builds: a second, smaller and shifted mesh is
+    keyed inside the first build's box, and the root given in is what an unlinked build
+    would leave."""
+    from libcl_gb300.scenes import triangle_soup
+    v, idx = triangle_soup(500, extent=2.0)
+    box_o, box_r = np.zeros(8, np.float32), np.zeros(8, np.float32)
+    oracle.bvh_build(v, idx, box_o)
+    ref.bvh_build(v, idx, box_r)
+    v2 = v.copy()
+    v2[:, :3] = v2[:, :3] * 0.25 + 3.0
+    _same_build(oracle.bvh_build(v2, idx, box_o, root=7), ref.bvh_build(v2, idx, box_r, root=7), "second build")
+    assert_same_bits(box_o, box_r, "global box after two builds")
+
+
+def test_bvh_reference_refuses_repeated_morton_keys():
+    """Two triangles with the same centroid share a Morton key; the reference's clLinkNodes
+    then lets two nodes claim one child, so the reference driver refuses the input (-5)."""
+    from libcl_gb300.scenes import triangle_soup
+    v, idx = triangle_soup(100)
+    idx = idx.copy()
+    idx[3:6] = idx[0:3]
+    rc = ref.bvh_build(v, idx, np.zeros(8, np.float32))[0]
+    assert rc == -5
+
+
+@pytest.mark.parametrize("scene", ["soup", "lattice"])
+def test_bvh_lines_build_matches_the_reference(scene):
+    """The 2D segment BVH: Morton keys of the truncated midpoints, the sort, linking, leaves
+    and boxes (every node's 32 bytes) and the root."""
+    from libcl_gb300.scenes import segment_lattice, segment_soup
+    v = segment_soup(5000) if scene == "soup" else segment_lattice(300)
+    _same_build(oracle.bvh_lines_build(v), ref.bvh_lines_build(v), scene)
 
 
 # ---------------------------------------------------------------------------------------
