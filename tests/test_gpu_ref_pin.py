@@ -1,7 +1,8 @@
 """GPU parity against the reference's own kernels (libCL/phys/oclFluid3D.cl,
-libCL/phys/oclFluid2D.cl, libCL/sort/oclRadixSort.cl built for the host cores by
-oracle/ref/build.py), run on the same inputs: the CUDA library's results must be the same
-bits. Skipped where those kernels are not built (oracle.ref.available())."""
+libCL/phys/oclFluid2D.cl, libCL/sort/oclRadixSort.cl, libCL/geom/oclBvhTrimesh.cl,
+libCL/geom/oclBvhLines.cl built for the host cores by oracle/ref/build.py), run on the same
+inputs: the CUDA library's results must be the same bits. Skipped where those kernels are not
+built (oracle.ref.available())."""
 import numpy as np
 import pytest
 
@@ -109,3 +110,31 @@ def test_emitter_equals_the_reference_kernel(cuda):
     ref.emit3d(pos, v, 200, 1.5, ref.system13(sc.params))
     same(g["pos"], pos, "positions")
     same(g["vel"], v, "velocities")
+
+
+def test_bvh_builds_equal_the_reference_kernels(cuda):
+    """gbsph_bvh (two builds on one handle: the global box carries over) and gbsph_bvh_lines
+    against oclBvhTrimesh::compute and oclBvhLines::compute run through the reference's
+    kernels: every node's bytes, the root and the box."""
+    import torch
+    from libcl_gb300 import BvhLines, BvhTrimesh
+    from libcl_gb300.scenes import segment_soup, sphere_mesh, triangle_soup
+    b = BvhTrimesh()
+    box = np.zeros(8, np.float32)
+    root = 0
+    for v, idx in (triangle_soup(3000), sphere_mesh(24, 48)):
+        b.compute(torch.from_numpy(v).cuda(), torch.from_numpy(idx.view(np.int32)).cuda())
+        assert b.sync_status() == 0
+        rc, nodes, root, _, _ = ref.bvh_build(v, idx, box, root)
+        assert rc == 0
+        same(b.getNodeBuffer().cpu().numpy().ravel(), nodes.view(np.uint32), "triangle BVH nodes")
+        assert b.getRootNode() == root
+        same(np.asarray(b.bounds(), np.float32), box, "global box")
+    lines = BvhLines()
+    v = segment_soup(5000)
+    lines.compute(torch.from_numpy(v).cuda())
+    assert lines.sync_status() == 0
+    rc, nodes, root, _, _ = ref.bvh_lines_build(v)
+    assert rc == 0
+    same(lines.getNodeBuffer().cpu().numpy().ravel(), nodes.view(np.uint32), "segment BVH nodes")
+    assert lines.getRootNode() == root
